@@ -1,0 +1,215 @@
+"""Python driver of the CPU oracle and of the host build of the reference.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py (CPU baseline / reference arm). The product package never imports it.
+
+* `cufd(...)` runs oracle/fwi_oracle.cpp (oracle/_build/liboracle_fwi.so), after
+  restating the reference's parameter and survey parsing (Parameter.cpp:16-178,
+  Src_Rec.cu:19-245) and its file I/O of observed data (libCUFD.cu:189-192,
+  514-521).
+* `refhost_cufd(...)` runs the reference's own sources compiled for the host
+  (oracle/_ref/librefhost_fwi.so, built by oracle/Makefile.refhost); it exists
+  only where the reference sources were available at build time.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(HERE, "_build", "liboracle_fwi.so")
+REFHOST_LIB = os.path.join(HERE, "_ref", "librefhost_fwi.so")
+
+
+class _Para(ctypes.Structure):
+    _fields_ = [("nz", ctypes.c_int), ("nx", ctypes.c_int), ("nSteps", ctypes.c_int), ("nPml", ctypes.c_int),
+                ("nPad", ctypes.c_int), ("dz", ctypes.c_float), ("dx", ctypes.c_float), ("dt", ctypes.c_float),
+                ("f0", ctypes.c_float), ("if_win", ctypes.c_int)]
+
+
+class _Shot(ctypes.Structure):
+    _fields_ = [("z_src", ctypes.c_int), ("x_src", ctypes.c_int), ("nrec", ctypes.c_int),
+                ("z_rec", ctypes.POINTER(ctypes.c_int)), ("x_rec", ctypes.POINTER(ctypes.c_int)),
+                ("win_start", ctypes.POINTER(ctypes.c_float)), ("win_end", ctypes.POINTER(ctypes.c_float)),
+                ("weights", ctypes.POINTER(ctypes.c_float))]
+
+
+_oracle = None
+_refhost = None
+
+
+def _load_oracle():
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(ORACLE_LIB):
+            raise RuntimeError(f"oracle library not built: {ORACLE_LIB} (run make -C oracle)")
+        lib = ctypes.CDLL(ORACLE_LIB)
+        lib.oracle_cufd.restype = ctypes.c_int
+        _oracle = lib
+    return _oracle
+
+
+def refhost_available() -> bool:
+    return os.path.exists(REFHOST_LIB)
+
+
+def _load_refhost():
+    global _refhost
+    if _refhost is None:
+        lib = ctypes.CDLL(REFHOST_LIB)
+        lib.refhost_cufd.restype = ctypes.c_int
+        _refhost = lib
+    return _refhost
+
+
+def read_first_line_json(path: str) -> dict:
+    """The reference parses only the first line of its JSON files (Parameter.cpp:28)."""
+    with open(path) as f:
+        return json.loads(f.readline())
+
+
+def load_para(path: str) -> dict:
+    """Parameter.cpp:16-178: required keys and optional switches."""
+    j = read_first_line_json(path)
+    for k in ("nz", "nx", "dz", "dx", "nSteps", "nPoints_pml", "nPad", "dt", "f0", "survey_fname", "data_dir_name"):
+        if k not in j:
+            raise KeyError(f"parameter file lacks {k}")
+    return {
+        "nz": int(j["nz"]), "nx": int(j["nx"]), "dz": float(j["dz"]), "dx": float(j["dx"]),
+        "nSteps": int(j["nSteps"]), "nPml": int(j["nPoints_pml"]), "nPad": int(j["nPad"]),
+        "dt": float(j["dt"]), "f0": float(j["f0"]), "survey_fname": j["survey_fname"],
+        "data_dir_name": j["data_dir_name"], "scratch_dir_name": j.get("scratch_dir_name"),
+        "if_win": bool(j.get("if_win", False)), "filter": j.get("filter"),
+        "if_src_update": bool(j.get("if_src_update", False)),
+    }
+
+
+def load_shots(survey_fname: str, shot_ids: Sequence[int], if_win: bool) -> list:
+    """Src_Rec.cu:80-200: per shot source / receiver indices (0-based interior)."""
+    s = read_first_line_json(survey_fname)
+    out = []
+    for sid in shot_ids:
+        d = s[f"shot{int(sid)}"]
+        shot = {"z_src": int(d["z_src"]), "x_src": int(d["x_src"]), "nrec": int(d["nrec"]),
+                "z_rec": np.asarray(d["z_rec"], dtype=np.int32)[: int(d["nrec"])],
+                "x_rec": np.asarray(d["x_rec"], dtype=np.int32)[: int(d["nrec"])]}
+        if if_win:
+            shot["win_start"] = np.asarray(d["win_start"], dtype=np.float32)
+            shot["win_end"] = np.asarray(d["win_end"], dtype=np.float32)
+            shot["weights"] = np.asarray(d["weights"], dtype=np.float32)
+        out.append(shot)
+    return out
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _iptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads: int = 0,
+         obs: Optional[Sequence[np.ndarray]] = None, write_files: bool = True, want_gathers: bool = False) -> dict:
+    """Oracle run of one `cufd` call (libCUFD.cu:34-580).
+
+    lam, mu [MPa] and den are row-major float64 [nz][nx]; stf is
+    [nShotsTotal][nSteps]. shot_ids are 0-based. For calc_id 0/1 observed data
+    are read from `data_dir_name/Shot<id>.bin` unless `obs` is given; for
+    calc_id 2 the gathers are written there when `write_files`.
+    Returns misfit, g_lambda, g_mu, g_den, g_stf and (optionally) gathers.
+    """
+    p = load_para(para_fname)
+    shot_ids = [int(v) for v in np.asarray(shot_ids).ravel()]
+    shots = load_shots(p["survey_fname"], shot_ids, p["if_win"])
+    nz, nx, nt = p["nz"], p["nx"], p["nSteps"]
+    lam = np.ascontiguousarray(lam, dtype=np.float64)
+    mu = np.ascontiguousarray(mu, dtype=np.float64)
+    den = np.ascontiguousarray(den, dtype=np.float64)
+    stf = np.ascontiguousarray(np.atleast_2d(stf), dtype=np.float64)
+    if lam.shape != (nz, nx) or mu.shape != (nz, nx) or den.shape != (nz, nx):
+        raise ValueError(f"model shape must be {(nz, nx)}")
+    para = _Para(nz, nx, nt, p["nPml"], p["nPad"], p["dz"], p["dx"], p["dt"], p["f0"], int(p["if_win"]))
+    keep = []
+    carr = (_Shot * len(shots))()
+    for i, s in enumerate(shots):
+        carr[i].z_src, carr[i].x_src, carr[i].nrec = s["z_src"], s["x_src"], s["nrec"]
+        zr = np.ascontiguousarray(s["z_rec"], dtype=np.int32)
+        xr = np.ascontiguousarray(s["x_rec"], dtype=np.int32)
+        keep += [zr, xr]
+        carr[i].z_rec, carr[i].x_rec = _iptr(zr), _iptr(xr)
+        if p["if_win"]:
+            ws, we, wt = (np.ascontiguousarray(s[k], dtype=np.float32) for k in ("win_start", "win_end", "weights"))
+            keep += [ws, we, wt]
+            carr[i].win_start, carr[i].win_end, carr[i].weights = _fptr(ws), _fptr(we), _fptr(wt)
+    n = len(shots)
+    obs_ptrs = (ctypes.POINTER(ctypes.c_float) * max(n, 1))()
+    if calc_id in (0, 1):
+        if obs is None:
+            obs = [np.fromfile(os.path.join(p["data_dir_name"], f"Shot{sid}.bin"), dtype=np.float32,
+                               count=s["nrec"] * nt) for sid, s in zip(shot_ids, shots)]
+        obs = [np.ascontiguousarray(o, dtype=np.float32).reshape(-1) for o in obs]
+        for i, o in enumerate(obs):
+            if o.size != shots[i]["nrec"] * nt:
+                raise ValueError("observed data of wrong size")
+            obs_ptrs[i] = _fptr(o)
+    syn = [np.zeros(s["nrec"] * nt, dtype=np.float32) for s in shots]
+    syn_ptrs = (ctypes.POINTER(ctypes.c_float) * max(n, 1))()
+    for i, a in enumerate(syn):
+        syn_ptrs[i] = _fptr(a)
+    misfit = ctypes.c_double(0.0)
+    g_lam = np.zeros((nz, nx))
+    g_mu = np.zeros((nz, nx))
+    g_den = np.zeros((nz, nx))
+    g_stf = np.zeros_like(stf)
+    ids = np.asarray(shot_ids, dtype=np.int32)
+    rc = _load_oracle().oracle_cufd(
+        ctypes.byref(para), carr, n, _iptr(ids), _dptr(lam), _dptr(mu), _dptr(den), _dptr(stf), int(calc_id),
+        obs_ptrs, syn_ptrs, None, ctypes.byref(misfit), _dptr(g_lam), _dptr(g_mu), _dptr(g_den), _dptr(g_stf),
+        int(nthreads))
+    if rc != 0:
+        raise RuntimeError(f"oracle_cufd failed with status {rc}")
+    out = {"misfit": misfit.value, "g_lambda": g_lam, "g_mu": g_mu, "g_den": g_den, "g_stf": g_stf}
+    gathers = [a.reshape(s["nrec"], nt) for a, s in zip(syn, shots)]
+    if calc_id == 2 and write_files:
+        for sid, a in zip(shot_ids, gathers):
+            a.astype(np.float32).tofile(os.path.join(p["data_dir_name"], f"Shot{sid}.bin"))
+    if want_gathers:
+        out["gathers"] = gathers
+    return out
+
+
+def refhost_cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str) -> dict:
+    """The reference driver itself (host build). Gathers of calc_id 2 are
+    written by it to data_dir_name and read back here."""
+    p = load_para(para_fname)
+    shot_ids = [int(v) for v in np.asarray(shot_ids).ravel()]
+    nz, nx, nt = p["nz"], p["nx"], p["nSteps"]
+    lam = np.ascontiguousarray(lam, dtype=np.float64)
+    mu = np.ascontiguousarray(mu, dtype=np.float64)
+    den = np.ascontiguousarray(den, dtype=np.float64)
+    stf = np.ascontiguousarray(np.atleast_2d(stf), dtype=np.float64)
+    misfit = ctypes.c_double(0.0)
+    g_lam = np.zeros((nz, nx))
+    g_mu = np.zeros((nz, nx))
+    g_den = np.zeros((nz, nx))
+    g_stf = np.zeros_like(stf)
+    ids = np.asarray(shot_ids, dtype=np.int32)
+    _load_refhost().refhost_cufd(ctypes.byref(misfit), _dptr(g_lam), _dptr(g_mu), _dptr(g_den), _dptr(g_stf),
+                                 _dptr(lam), _dptr(mu), _dptr(den), _dptr(stf), int(calc_id), len(shot_ids),
+                                 _iptr(ids), para_fname.encode())
+    out = {"misfit": misfit.value, "g_lambda": g_lam, "g_mu": g_mu, "g_den": g_den, "g_stf": g_stf}
+    if calc_id == 2:
+        shots = load_shots(p["survey_fname"], shot_ids, False)
+        out["gathers"] = [np.fromfile(os.path.join(p["data_dir_name"], f"Shot{sid}.bin"), dtype=np.float32,
+                                      count=s["nrec"] * nt).reshape(s["nrec"], nt)
+                          for sid, s in zip(shot_ids, shots)]
+    return out
