@@ -1,0 +1,339 @@
+"""Benchmark of the GB300 elastic FWI operator: batched forward + adjoint
+throughput (Gpts/s = grid cells x time steps x shots per second of one
+misfit + gradient evaluation) against the HBM roofline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload dipping_grf|small_layered] [--no-cpu-baseline]
+
+One step = one misfit + gradient call (forward sweep with boundary saving,
+residual, reverse / adjoint sweeps with imaging) over the workload's shots.
+`value`: model, shots and observed data resident in HBM, CUDA events on the
+library's stream around fwigb_run. `e2e`: the public C-ABI call
+fwigb_misfit_grad_obs with pinned host buffers (model in, gradients out).
+`--impl reference` times the reference algorithm's CPU implementation (the
+oracle restatement, all host threads) on a bounded number of time steps of
+the same workload. With N > 1 (torchrun) every rank runs its own replica.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as ge  # noqa: E402
+
+# Algorithmic bytes per grid cell and time step of each sweep (FP32 arrays read
+# or written once): forward stress 11 floats, forward velocity 9, backward B 24,
+# backward C 22; forward + adjoint = 264 B per cell-step.
+SWEEP_NAMES = ["fwd_stress", "fwd_velocity", "bwd_B", "bwd_C"]
+SWEEP_KERNELS = ["k_fwd_stress", "k_fwd_velocity", "k_bwd_B", "k_bwd_C"]
+SWEEP_BYTES = [44, 36, 96, 88]
+FWD_ADJ_BYTES = 264
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(name):
+    fw = ge.load_package()
+    from fwiflow_gb300 import synthetic
+
+    if name == "small_layered":
+        return synthetic.small_layered()
+    return synthetic.dipping_grf()
+
+
+def describe(w):
+    return (f"{w.name}: {w.nz}x{w.nx} interior + {w.nPml} CPML (nPad {w.nPad}) = {w.nz_pad}x{w.nx_pad} cells, "
+            f"{w.nSteps} steps, {len(w.shots)} shot(s), dx {w.dx} m, dt {w.dt * 1e3:g} ms, FP32; "
+            f"one misfit+gradient per step")
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 8:
+                    continue
+                try:
+                    sm.append(float(parts[0]))
+                    smax.append(float(parts[1]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[4:8]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_cpu_oracle(w, n_steps_sample, reps=1):
+    """Times the oracle (reference algorithm on the host cores) on the first
+    n_steps_sample time steps of the workload; returns (Gpts/s, seconds, threads)."""
+    orc = ge.load_oracle()
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    from dataclasses import replace
+
+    ws = replace(w, nSteps=n_steps_sample, stf=np.ascontiguousarray(w.stf[:, :n_steps_sample]))
+    tmp = tempfile.mkdtemp()
+    para = ws.write_files(tmp)
+    ids = list(range(len(ws.shots)))
+    nthreads = cpu_threads()
+    orc.cufd(2, *ws.moduli(ws.vp_obs), ws.stf, ids, para, nthreads=nthreads)  # observed data, untimed
+    lam, mu, rho = ws.moduli()
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        orc.cufd(1, lam, mu, rho, ws.stf, ids, para, nthreads=nthreads)
+        orc.cufd(0, lam, mu, rho, ws.stf, ids, para, nthreads=nthreads)
+        times.append(time.perf_counter() - t0)
+    pts = ws.cells * n_steps_sample * len(ids)
+    return pts / min(times) / 1e9, times, nthreads
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="dipping_grf", choices=["dipping_grf", "small_layered"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-steps", type=int, default=200)
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    w = workload(args.workload)
+    metric, unit = "fwd+adj Gpts/s vs HBM roofline", "Gpts/s"
+    cfg = {"workload": describe(w), "cells": w.cells, "nSteps": w.nSteps, "shots": len(w.shots),
+           "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+           "l2": "flushed between timed steps (256 MiB write); each step also streams a "
+                 f"{w.nSteps * 5 * 4 * (10 * (w.nx_pad - 2 * w.nPml + 4) + 10 * (w.nz_pad - 2 * w.nPml - w.nPad - 6)) / 2**30:.2f}"
+                 " GiB boundary store"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        n_sample = max(20, min(args.cpu_sample_steps, w.nSteps) // 2)
+        vals = []
+        for _ in range(args.warmup):
+            run_cpu_oracle(w, n_sample)
+        t_all = []
+        for _ in range(args.steps):
+            g, t, threads = run_cpu_oracle(w, n_sample)
+            vals.append(g)
+            t_all += t
+        value = statistics.median(vals)
+        sample = (f"first {n_sample} of {w.nSteps} time steps of the same grid and shots, misfit + gradient "
+                  f"(oracle restatement of the reference cufd path, OpenMP)")
+        line = {"impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(t_all),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": cfg,
+                "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": "port", "sample": sample},
+                "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    fw = ge.load_package()
+    ge._build_lib()
+    tmp = tempfile.mkdtemp()
+    para = w.write_files(tmp)
+    ctx = fw.FwiContext(para, local_rank)
+    ids = list(range(len(w.shots)))
+    obs = ctx.obs(*w.moduli(w.vp_obs), w.stf, ids, write_files=False)
+    lam, mu, rho = w.moduli()
+    ctx.set_model(lam, mu, rho)
+    ctx.stage_shots(w.stf, ids, obs=obs)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local_rank))
+    flush = torch.empty(64 * 2 ** 20, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        ctx.run(1)
+    ctx.synchronize()
+    clocks = ClockSampler(local_rank)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stops = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            ctx.run(1)
+            stops[k].record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches_per_step = ctx.last_launch_count()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, stops)]
+    dev_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([dev_s, wall], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s, wall = float(t[0]), float(t[1])
+    pts_step = w.cells * w.nSteps * len(ids)
+    value = world * pts_step * args.steps / dev_s / 1e9
+
+    # Per-kernel event timing (one instrumented step) for the roofline.
+    ctx.set_kernel_timing(True)
+    ctx.run(1)
+    tot, cnt = ctx.kernel_times()
+    ctx.set_kernel_timing(False)
+    k_dom = int(np.argmax(tot))
+    avg_s = tot[k_dom] / cnt[k_dom] / 1e3
+    peak, peak_kind = peaks()
+    achieved = SWEEP_BYTES[k_dom] * w.cells / avg_s / 1e9
+    per_kernel = {SWEEP_NAMES[k]: {"launches": int(cnt[k]), "avg_us": 1e3 * tot[k] / max(cnt[k], 1),
+                                   "share": float(tot[k] / tot.sum()),
+                                   "algorithmic_GBps": SWEEP_BYTES[k] * w.cells / (tot[k] / max(cnt[k], 1) / 1e3) / 1e9}
+                  for k in range(4)}
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if os.path.exists(tfile):
+        for line in open(tfile):
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == SWEEP_KERNELS[k_dom] and not line.startswith("#"):
+                traffic = float(parts[1]) * w.cells / float(parts[2])
+    step_gbps = FWD_ADJ_BYTES * pts_step / (dev_s / args.steps) / 1e9
+
+    # End to end through the public C ABI with pinned host buffers.
+    def pinned(a, dtype):
+        t = torch.empty(a.shape, dtype=dtype, pin_memory=True)
+        t.numpy()[...] = a
+        return t.numpy()
+
+    lam_h, mu_h, rho_h = (pinned(a, torch.float64) for a in (lam, mu, rho))
+    stf_h = pinned(w.stf, torch.float64)
+    obs_blk = np.zeros((len(ids), ctx.nrec_max, w.nSteps), dtype=np.float32)
+    for i, o in enumerate(obs):
+        obs_blk[i, :o.shape[0]] = o
+    obs_h = pinned(obs_blk, torch.float32)
+    out = {k: pinned(np.zeros((w.nz_pad, w.nx_pad)), torch.float64) for k in ("gl", "gm", "gd")}
+    gs_h = pinned(np.zeros((len(ids), w.nSteps)), torch.float64)
+    mis = np.zeros(1)
+    lib = ctx._lib
+    from fwiflow_gb300 import _lib
+
+    ids_a = np.asarray(ids, dtype=np.int32)
+
+    def e2e_call():
+        _lib.check(lib.fwigb_misfit_grad_obs(ctx._h, _lib.dptr(lam_h), _lib.dptr(mu_h), _lib.dptr(rho_h),
+                                             _lib.dptr(stf_h), stf_h.shape[0], _lib.iptr(ids_a), len(ids),
+                                             _lib.fptr(obs_h), _lib.dptr(mis), _lib.dptr(out["gl"]),
+                                             _lib.dptr(out["gm"]), _lib.dptr(out["gd"]), _lib.dptr(gs_h)), ctx._h)
+
+    e2e_call()
+    barrier()
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_call()
+    barrier()
+    e2e_s = time.perf_counter() - t1
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t[0])
+    e2e_val = world * pts_step * args.steps / e2e_s / 1e9
+    h2d = 3 * w.cells * 8 + stf_h.nbytes + obs_h.nbytes
+    d2h = 3 * w.cells * 8 + len(ids) * w.nSteps * 4 + 8
+
+    if rank != 0:
+        return
+    line = {
+        "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dev_s / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": cfg,
+        "roofline": {"bound": "hbm", "kernel": SWEEP_KERNELS[k_dom], "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
+                     if peak_kind == "measured" else "fallback 6.8 TB/s",
+                     "traffic": traffic, "algorithmic_bytes_per_launch": SWEEP_BYTES[k_dom] * w.cells,
+                     "step_algorithmic_GBps": step_gbps, "step_frac": step_gbps / peak, "kernels": per_kernel},
+        "e2e": {"value": e2e_val, "unit": unit, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches_per_step * args.steps),
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        g, t, threads = run_cpu_oracle(w, min(args.cpu_sample_steps, w.nSteps))
+        line["cpu_baseline"] = {"value": g, "unit": unit, "cores": threads, "kind": "port",
+                                "sample": f"first {min(args.cpu_sample_steps, w.nSteps)} of {w.nSteps} time steps, "
+                                          f"same grid and shots, misfit + gradient, {t[0]:.1f} s"}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,111 @@
+// Device-side data structures of the GB300 elastic FWI engine and the host
+// launch interface of its kernels (implemented in kernels.cu).
+//
+// Layout in HBM: every grid array is column-major [nx][nz] float, z fastest,
+// as in the reference (a(z,x) = a[x*nz + z], el_stress.cu:1-19), so one warp
+// reads 32 consecutive depths of one column in a single 128-byte transaction.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace fwigb {
+
+// Thread-block tile of the grid sweeps: 32 depths (one warp) x kTileX columns.
+constexpr int kTileZ = 32;
+constexpr int kTileX = 8;
+
+// Grid geometry and the index ranges of the reference kernels.
+struct Geo {
+  int nz, nx, nPml, nPad;
+  int zs0, zs1, xs0, xs1;  // stencil domain [2, nz-nPad-3] x [2, nx-3] (el_stress.cu:52)
+  int zi0, zi1, xi0, xi1;  // reverse-time interior (el_stress.cu:93)
+  int zpml_hi;             // z-PML: z < nPml || z > zpml_hi   (= nz-nPml-nPad-1)
+  int xpml_hi_s;           // stress / adjoint x-PML: x > xpml_hi_s (= nx-nPml-1)
+  int xpml_hi_v;           // forward velocity x-PML: x > xpml_hi_v (= nx-nPml, el_velocity.cu:56)
+  int xband_lo, xband_hi;  // adjoint memory band in x: x <= xband_lo || x >= xband_hi
+  int zband_lo, zband_hi;  // adjoint memory band in z
+  // Boundary ring saved each forward step: box [rz0,rz1]x[rx0,rx1] minus its
+  // inner box shrunk by 5 (the 5 layers around the interior, Boundary.cu:17-27).
+  int rz0, rz1, rx0, rx1, ringW, ringH, ring_len;
+  float dt, rdz, rdx;
+};
+
+struct Fields {
+  float *vz, *vx, *szz, *sxx, *sxz;
+  float *vz_a, *vx_a, *szz_a, *sxx_a, *sxz_a;
+  float *m_dvz_dz, *m_dvz_dx, *m_dvx_dz, *m_dvx_dx;    // forward CPML / adjoint psi memory
+  float *m_dszz_dz, *m_dsxx_dx, *m_dsxz_dz, *m_dsxz_dx;  // forward CPML / adjoint phi memory
+};
+
+struct MediaD {
+  const float* lam;    // lambda [Pa]
+  const float* l2m;    // lambda + 2 mu [Pa]
+  const float* aveMu;  // harmonic 2x2 average of mu (aveMuInit, utilities.cu:125-140)
+  const float* bycA;   // 2 / (rho(z) + rho(z+1))  (aveBycInit, utilities.cu:142-152)
+  const float* bycB;   // 2 / (rho(x) + rho(x+1))
+  const float* hs;     // aveMu / sum(1/mu over the 2x2 block) * 1e6, 0 where aveMu == 0
+  const float* muw;    // 1 / mu^2, 0 where mu == 0
+};
+
+struct CpmlD {
+  const float *K_z, *a_z, *b_z, *K_zh, *a_zh, *b_zh;  // length nz
+  const float *K_x, *a_x, *b_x, *K_xh, *a_xh, *b_xh;  // length nx
+};
+
+// Per-shot data for the sweeps.
+struct ShotD {
+  int src_z, src_x;       // source cell (padded-grid indices)
+  const float* src_szz;   // per step: 1500^2 * amp * dt (add_source, utilities.cu:528-538)
+  const float* src_sxx;   // per step: 3 * 1500^2 * amp * dt
+  int nrec, nSteps;
+  const int* rec_z;       // receiver cells
+  const int* rec_x;
+  const int* blk_off;     // receivers per thread block (CSR over the sweep grid)
+  const int* blk_rec;
+  float* data;            // synthetic gathers [nrec][nSteps]
+  const float* res;       // adjoint source [nrec][nSteps]
+  float* gstf;            // source-time-function gradient [nSteps]
+};
+
+struct StoreD {
+  float* base;  // [step][5 fields: szz, sxz, sxx, vz, vx][ring_len]
+};
+
+struct Grads {
+  float* lam;
+  float* mu;
+  float* den;
+};
+
+// ---- launchers (kernels.cu) ----
+void launch_fwd_stress(cudaStream_t s, const Geo& g, const Fields& f, const MediaD& m, const CpmlD& c,
+                       const ShotD& sh, const StoreD& st, int it, bool save);
+void launch_fwd_velocity(cudaStream_t s, const Geo& g, const Fields& f, const MediaD& m, const CpmlD& c);
+void launch_bwd_B(cudaStream_t s, const Geo& g, const Fields& f, const MediaD& m, const CpmlD& c, const ShotD& sh,
+                  const StoreD& st, const Grads& gr, int it);
+void launch_bwd_C(cudaStream_t s, const Geo& g, const Fields& f, const MediaD& m, const CpmlD& c, const ShotD& sh,
+                  const StoreD& st, const Grads& gr, int it, bool rev);
+
+// Model set-up: row-major double (lambda, mu in MPa) -> column-major float media.
+// cpmax_bits receives atomicMax of the P velocity's float bits.
+void launch_media_from_rowmajor(cudaStream_t s, int nz, int nx, const double* lam_mpa, const double* mu_mpa,
+                                const double* den, float* lam, float* mu, float* den_f, unsigned* cpmax_bits);
+void launch_media_derived(cudaStream_t s, int nz, int nx, const float* lam, const float* mu, const float* den,
+                          float* l2m, float* aveMu, float* bycA, float* bycB, float* hs, float* muw,
+                          unsigned* cpmax_bits);
+
+// Residual: res = taper_r * (taper_o * obs - taper_o * syn) with sample 0
+// zeroed; syn is tapered in place. taper arrays are [nrec][nSteps] when
+// per_trace, else [nSteps]. Block partial sums of res^2 (before the adjoint
+// taper) go to partials[0..nblocks).
+int residual_blocks(int n);
+void launch_residual(cudaStream_t s, int nrec, int nSteps, const float* obs, float* syn, float* res,
+                     const float* taper_o, const float* taper_r, int per_trace, double* partials);
+void launch_sum_partials(cudaStream_t s, const double* partials, int n, double* acc);
+
+// Column-major float grid -> row-major double.
+void launch_to_rowmajor(cudaStream_t s, int nz, int nx, const float* src, double* dst, double scale);
+
+}  // namespace fwigb

@@ -1,0 +1,153 @@
+/*
+ * fwiflow_gb300.h — C ABI of the GB300 (sm_103a) elastic FWI operator.
+ *
+ * Drop-in for the FWI operator of FwiFlow.jl: the same inputs, units, layouts
+ * and outputs as the reference driver
+ *
+ *   void cufd(double *misfit, double *grad_Lambda, double *grad_Mu,
+ *             double *grad_Den, double *grad_stf, const double *Lambda,
+ *             const double *Mu, const double *Den, const double *stf,
+ *             int calc_id, const int gpu_id, int group_size,
+ *             const int *shot_ids, const std::string para_fname);
+ *   (deps/CustomOps/FWI/Src/libCUFD.cu:34-38)
+ *
+ * and of the TensorFlow ops built on it, FwiOp / FwiOpGrad / FwiObsOp
+ * (deps/CustomOps/FWI/FwiOp.cpp:15-319, FwiOp.h:14-34), which the Julia
+ * functions fwi_op / fwi_obs_op bind (src/Core.jl:20-53).
+ *
+ * Conventions (all as in the reference):
+ *  - lambda, mu in MPa and den in kg/m^3 are row-major double [nz][nx] on the
+ *    padded grid of the parameter file (nz, nx there include the PML and nPad);
+ *  - stf is row-major double [n_stf_rows][nSteps]; row shot_ids[i] drives
+ *    shot i; shot_ids are 0-based and name `shot<k>` entries of the survey file;
+ *  - gradients are w.r.t. lambda and mu in MPa and den, accumulated over all
+ *    shots of the call; g_stf row i belongs to the i-th shot of the call;
+ *  - misfit = 0.5 * sum over shots, receivers and samples 1..nSteps-1 of the
+ *    squared tapered residual;
+ *  - observed data come from data_dir_name/Shot<id>.bin ([nrec][nSteps] f32)
+ *    unless passed in memory.
+ * Every call returns an fwigb_status; nothing calls exit(). The library
+ * allocates its device buffers itself and keeps them in the context.
+ */
+#ifndef FWIFLOW_GB300_H_
+#define FWIFLOW_GB300_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum fwigb_status {
+  FWIGB_OK = 0,
+  FWIGB_ERR_ARG = 1,        /* bad argument (null pointer, size mismatch, bad calc_id) */
+  FWIGB_ERR_PARAM = 2,      /* parameter or survey file unreadable / missing key */
+  FWIGB_ERR_COURANT = 3,    /* Courant number > 1 (the reference exits, utilities.cu:239) */
+  FWIGB_ERR_CUDA = 4,       /* CUDA runtime error */
+  FWIGB_ERR_OOM = 5,        /* device allocation failed */
+  FWIGB_ERR_IO = 6,         /* observed-data or output file I/O failed */
+  FWIGB_ERR_TIMEOUT = 7,    /* a bounded device wait gave up */
+  FWIGB_ERR_UNSUPPORTED = 8 /* option of the parameter file this build does not implement */
+} fwigb_status;
+
+typedef struct fwigb_ctx fwigb_ctx;
+
+/* Opens a context for one parameter file on one CUDA device. Replaces the
+ * per-call set-up of cufd (libCUFD.cu:42-93: cudaSetDevice, Parameter, Model,
+ * Cpml, Bnd, Src_Rec); the context keeps parsed geometry and device buffers
+ * across calls. */
+int fwigb_create(const char *para_fname, int device, fwigb_ctx **out);
+
+/* Releases a context and its device memory. */
+int fwigb_destroy(fwigb_ctx *ctx);
+
+/* Message of the last failure on this context (never NULL). */
+const char *fwigb_last_error(const fwigb_ctx *ctx);
+
+/* Message of the last failure of fwigb_create / fwigb_cufd (thread-local). */
+const char *fwigb_last_global_error(void);
+
+/* FwiOp forward: misfit only (cufd calc_id 0; FwiOp.cpp:47-103). */
+int fwigb_misfit(fwigb_ctx *ctx, const double *lambda, const double *mu, const double *den, const double *stf,
+                 int n_stf_rows, const int *shot_ids, int n_shots, double *misfit);
+
+/* FwiOpGrad (cufd calc_id 1; FwiOp.cpp:130-223), computed with a single
+ * forward sweep: misfit (may be NULL) and the four gradients. g_stf has
+ * n_shots rows of nSteps (the reference writes only the first group rows of
+ * its [n_stf_rows][nSteps] output, libCUFD.cu:452-456). */
+int fwigb_misfit_grad(fwigb_ctx *ctx, const double *lambda, const double *mu, const double *den, const double *stf,
+                      int n_stf_rows, const int *shot_ids, int n_shots, double *misfit, double *g_lambda,
+                      double *g_mu, double *g_den, double *g_stf);
+
+/* FwiObsOp (cufd calc_id 2; FwiOp.cpp:260-317): forward modelling only.
+ * gathers (may be NULL) receives shot i at offset i*nrec_max*nSteps as
+ * [nrec][nSteps] float; write_files != 0 also writes data_dir_name/Shot<id>.bin
+ * exactly as libCUFD.cu:514-521. */
+int fwigb_obs(fwigb_ctx *ctx, const double *lambda, const double *mu, const double *den, const double *stf,
+              int n_stf_rows, const int *shot_ids, int n_shots, float *gathers, int write_files);
+
+/* Variant of fwigb_misfit / fwigb_misfit_grad taking observed data from
+ * memory: obs holds shot i at offset i*nrec_max*nSteps as [nrec][nSteps]. */
+int fwigb_misfit_grad_obs(fwigb_ctx *ctx, const double *lambda, const double *mu, const double *den,
+                          const double *stf, int n_stf_rows, const int *shot_ids, int n_shots, const float *obs,
+                          double *misfit, double *g_lambda, double *g_mu, double *g_den, double *g_stf);
+
+/* Geometry of the context: nz, nx, nSteps, number of shots in the survey and
+ * the largest receiver count of any shot. */
+int fwigb_geometry(const fwigb_ctx *ctx, int *nz, int *nx, int *nSteps, int *n_survey_shots, int *nrec_max);
+
+/* Number of receivers of survey shot `shot_id`. */
+int fwigb_shot_nrec(const fwigb_ctx *ctx, int shot_id, int *nrec);
+
+/* One-call drop-in for cufd itself (libCUFD.cu:34-38) with a C string for the
+ * parameter file. calc_id 0 writes misfit, 1 writes the gradients (g_stf has
+ * group_size rows), 2 writes Data/Shot<id>.bin. A context per (para_fname,
+ * gpu_id) is cached and reused by later calls. */
+int fwigb_cufd(double *misfit, double *grad_Lambda, double *grad_Mu, double *grad_Den, double *grad_stf,
+               const double *Lambda, const double *Mu, const double *Den, const double *stf, int calc_id,
+               int gpu_id, int group_size, const int *shot_ids, const char *para_fname);
+
+/* ---- Staged interface: the calls above are set_model + stage_shots + run +
+ * fetch. Keeping the model and the shots resident lets a caller (and the
+ * benchmark) run the device part alone. ---- */
+
+/* Uploads lambda, mu [MPa] and den (row-major double [nz][nx]), derives the
+ * staggered media and checks the Courant number (libCUFD.cu:67-96). */
+int fwigb_set_model(fwigb_ctx *ctx, const double *lambda, const double *mu, const double *den);
+
+/* Stages the shots of a call: source rows of stf, receivers, and (when
+ * with_obs) observed data, from `obs` ([n_shots][nrec_max][nSteps] float, may
+ * be NULL) or else from data_dir_name/Shot<id>.bin. */
+int fwigb_stage_shots(fwigb_ctx *ctx, const double *stf, int n_stf_rows, const int *shot_ids, int n_shots,
+                      int with_obs, const float *obs);
+
+/* Runs the staged shots on the device, asynchronously on the context's
+ * stream. calc_id 0: misfit, 1: misfit and gradients, 2: gathers only. */
+int fwigb_run(fwigb_ctx *ctx, int calc_id);
+
+/* Copies results of the last run to the host (synchronises). Any pointer may
+ * be NULL. g_stf has n_shots rows of nSteps. gathers as in fwigb_obs. */
+int fwigb_fetch(fwigb_ctx *ctx, double *misfit, double *g_lambda, double *g_mu, double *g_den, double *g_stf,
+                float *gathers);
+
+/* Waits for the context's stream. */
+int fwigb_synchronize(fwigb_ctx *ctx);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that time it. */
+void *fwigb_stream(fwigb_ctx *ctx);
+
+/* Number of kernel launches the last fwigb_run issued (host-side count). */
+long long fwigb_last_launch_count(const fwigb_ctx *ctx);
+
+/* Per-kernel timing of fwigb_run: when enabled, a CUDA event pair on the
+ * context's stream brackets every sweep launch. Kinds: 0 forward stress,
+ * 1 forward velocity, 2 backward sweep B, 3 backward sweep C. */
+int fwigb_set_kernel_timing(fwigb_ctx *ctx, int enable);
+
+/* Totals of the timed launches of the last fwigb_run (synchronises):
+ * total_ms[4] and launches[4], indexed by kind. */
+int fwigb_kernel_times(fwigb_ctx *ctx, double *total_ms, long long *launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FWIFLOW_GB300_H_ */

@@ -1,0 +1,115 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+The reference FWI core (FwiFlow.jl deps/CustomOps/FWI/Src) is compiled for the
+host CPU by oracle/Makefile.refhost (its CUDA kernels run under the emulation
+shim in oracle/refhost/) and driven through its own `cufd` entry point with
+parameter / survey / Data files written by the package's paraGen / surveyGen.
+Run from the repository root, where the reference sources are available:
+
+    make -C oracle -f Makefile.refhost REF=/path/to/FwiFlow.jl
+    python tests/golden/make_golden.py
+
+Cases (all seeded, see fwiflow.jl_gb300/synthetic.py):
+  tiny_elastic   32x48 interior, nPml 10, 200 steps, 2 shots: gathers, misfit, gradients
+  tiny_acoustic  same geometry with Vs = 0 and constant density (the mu == 0 path)
+  tiny_window    1 shot with per-trace windows and weights (if_win, utilities.cu:653-705)
+  small_layered  the 100x200, 1000-step, 2-shot workload: misfit, norms and a strided
+                 subsample of gathers and gradients
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as ge  # noqa: E402
+
+fw = ge.load_package()
+orc = ge.load_oracle()
+from fwiflow_gb300 import synthetic  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+STRIDE = 16
+
+
+def run_case(w, with_window=False):
+    tmp = tempfile.mkdtemp()
+    if with_window:
+        rng = np.random.default_rng(7)
+        for s in w.shots:
+            n = len(s["x_rec"])
+            T = w.nSteps * w.dt
+            s["win_start"] = list(rng.uniform(0.0, 0.2 * T, n))
+            s["win_end"] = list(rng.uniform(0.6 * T, 1.1 * T, n))
+            s["weights"] = list(rng.uniform(0.5, 1.5, n))
+        para = w.write_files(tmp)
+        p = json.load(open(para))
+        p["if_win"] = True
+        with open(para, "w") as f:
+            f.write(json.dumps(p, separators=(",", ":")))
+    else:
+        para = w.write_files(tmp)
+    moduli = (lambda v: synthetic.tiny_moduli(w, v)) if w.name == "tiny" else w.moduli
+    lo, mo, ro = moduli(w.vp_obs)
+    lam, mu, rho = moduli(w.vp)
+    ids = list(range(len(w.shots)))
+    r2 = orc.refhost_cufd(2, lo, mo, ro, w.stf, ids, para)
+    r0 = orc.refhost_cufd(0, lam, mu, rho, w.stf, ids, para)
+    r1 = orc.refhost_cufd(1, lam, mu, rho, w.stf, ids, para)
+    return para, r2, r0, r1
+
+
+def save_full(name, w, r2, r0, r1, **meta):
+    np.savez_compressed(
+        os.path.join(OUT, f"{name}.npz"),
+        gathers=np.stack(r2["gathers"]).astype(np.float32),
+        misfit=np.float64(r0["misfit"]),
+        g_lambda=r1["g_lambda"].astype(np.float32),
+        g_mu=r1["g_mu"].astype(np.float32),
+        g_den=r1["g_den"].astype(np.float32),
+        g_stf=r1["g_stf"].astype(np.float32),
+        meta=json.dumps(meta),
+    )
+
+
+def main():
+    if not orc.refhost_available():
+        raise SystemExit("oracle/_ref/librefhost_fwi.so missing: build it with oracle/Makefile.refhost")
+    w = synthetic.tiny(nz=32, nx=48, nPml=10, nSteps=200, n_shots=2, seed=0)
+    _, r2, r0, r1 = run_case(w)
+    save_full("tiny_elastic", w, r2, r0, r1, builder="tiny", kwargs=dict(nz=32, nx=48, nPml=10, nSteps=200,
+                                                                            n_shots=2, seed=0))
+    w = synthetic.tiny(nz=32, nx=48, nPml=10, nSteps=200, n_shots=2, seed=1, cs_zero=True)
+    _, r2, r0, r1 = run_case(w)
+    save_full("tiny_acoustic", w, r2, r0, r1, builder="tiny", kwargs=dict(nz=32, nx=48, nPml=10, nSteps=200,
+                                                                             n_shots=2, seed=1, cs_zero=True))
+    w = synthetic.tiny(nz=32, nx=48, nPml=10, nSteps=200, n_shots=1, seed=2)
+    _, r2, r0, r1 = run_case(w, with_window=True)
+    save_full("tiny_window", w, r2, r0, r1, builder="tiny", window_seed=7,
+              kwargs=dict(nz=32, nx=48, nPml=10, nSteps=200, n_shots=1, seed=2))
+    w = synthetic.small_layered()
+    _, r2, r0, r1 = run_case(w)
+    g = np.stack(r2["gathers"]).astype(np.float32)
+    np.savez_compressed(
+        os.path.join(OUT, "small_layered.npz"),
+        stride=np.int64(STRIDE),
+        misfit=np.float64(r0["misfit"]),
+        gathers_sub=g.reshape(-1)[::STRIDE],
+        gathers_norm=np.float64(np.linalg.norm(g.astype(np.float64))),
+        g_lambda_sub=r1["g_lambda"].reshape(-1)[::STRIDE].astype(np.float32),
+        g_mu_sub=r1["g_mu"].reshape(-1)[::STRIDE].astype(np.float32),
+        g_den_sub=r1["g_den"].reshape(-1)[::STRIDE].astype(np.float32),
+        g_norms=np.array([np.linalg.norm(r1[k]) for k in ("g_lambda", "g_mu", "g_den", "g_stf")]),
+        g_stf=r1["g_stf"].astype(np.float32),
+        meta=json.dumps({"builder": "small_layered"}),
+    )
+    print("golden fixtures written to", OUT)
+
+
+if __name__ == "__main__":
+    main()

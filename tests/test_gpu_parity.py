@@ -1,0 +1,105 @@
+"""Parity of the sm_103a CUDA path with the reference (golden fixtures made by
+the reference's own sources) and with the CPU oracle, through the C ABI.
+
+Tolerances (FP32 throughout; the reference promotes some products to double):
+gathers and misfit within 1e-4 relative L2, gradients within 1e-3.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_workload, rel
+
+pytestmark = pytest.mark.gpu
+
+TOL_DATA = 1e-4
+TOL_GRAD = 1e-3
+
+
+@pytest.mark.parametrize("name", ["tiny_elastic", "tiny_acoustic", "tiny_window"])
+def test_cuda_matches_reference_golden(name, gpu_lib, fw, tmp_path):
+    d, w, para, moduli = golden_workload(name, tmp_path)
+    ids = list(range(len(w.shots)))
+    ctx = fw.FwiContext(para, 0)
+    lo, mo, ro = moduli(w.vp_obs)
+    g = ctx.obs(lo, mo, ro, w.stf, ids, write_files=True)
+    assert rel(np.stack(g), d["gathers"]) < TOL_DATA
+    lam, mu, rho = moduli(w.vp)
+    J = ctx.misfit(lam, mu, rho, w.stf, ids)
+    assert abs(J - float(d["misfit"])) <= TOL_DATA * abs(float(d["misfit"]))
+    J2, gl, gm, gd, gs = ctx.misfit_grad(lam, mu, rho, w.stf, ids)
+    assert abs(J2 - J) <= 1e-6 * abs(J)  # one forward pass gives the same misfit
+    assert rel(gl, d["g_lambda"]) < TOL_GRAD
+    assert rel(gd, d["g_den"]) < TOL_GRAD
+    assert rel(gs, d["g_stf"]) < TOL_GRAD
+    if name == "tiny_acoustic":
+        assert np.abs(gm).max() == 0.0 or rel(gm, d["g_mu"]) < TOL_GRAD
+    else:
+        assert rel(gm, d["g_mu"]) < TOL_GRAD
+    ctx.close()
+
+
+def test_cuda_matches_reference_golden_small_layered(gpu_lib, fw, tmp_path):
+    """The 100x200-interior, 1000-step, 2-shot workload (padded 192x264)."""
+    d, w, para, _ = golden_workload("small_layered", tmp_path)
+    ids = [0, 1]
+    s = int(d["stride"])
+    ctx = fw.FwiContext(para, 0)
+    g = np.stack(ctx.obs(*w.moduli(w.vp_obs), w.stf, ids, write_files=True))
+    assert rel(g.reshape(-1)[::s], d["gathers_sub"]) < TOL_DATA
+    assert abs(np.linalg.norm(g.astype(np.float64)) - float(d["gathers_norm"])) < TOL_DATA * float(d["gathers_norm"])
+    J, gl, gm, gd, gs = ctx.misfit_grad(*w.moduli(), w.stf, ids)
+    assert abs(J - float(d["misfit"])) <= TOL_DATA * abs(float(d["misfit"]))
+    for k, a in (("g_lambda", gl), ("g_mu", gm), ("g_den", gd)):
+        assert rel(a.reshape(-1)[::s], d[k + "_sub"]) < TOL_GRAD, k
+    assert rel(gs, d["g_stf"]) < TOL_GRAD
+    ctx.close()
+
+
+@pytest.mark.parametrize("case", [
+    dict(nz=20, nx=33, nPml=6, nSteps=120, n_shots=1, seed=3),
+    dict(nz=37, nx=70, nPml=9, nSteps=160, n_shots=3, seed=4),
+    dict(nz=64, nx=40, nPml=16, nSteps=200, n_shots=2, seed=5),
+])
+def test_cuda_matches_oracle_irregular(case, gpu_lib, fw, orc, tmp_path):
+    """Odd sizes (partial tiles), receivers at irregular depths with one
+    duplicated cell, sources near the interior edge."""
+    from fwiflow_gb300 import synthetic
+
+    w = synthetic.tiny(**case)
+    for k, s in enumerate(w.shots):
+        s["z_rec"] = [(r * 7) % (w.nz - 1) for r in range(len(s["x_rec"]))]
+        s["x_rec"][1] = s["x_rec"][0]
+        s["z_rec"][1] = s["z_rec"][0]
+        s["x_src"] = 0 if k == 0 else s["x_src"]
+    para = w.write_files(str(tmp_path))
+    ids = list(range(len(w.shots)))
+    lo, mo, ro = w.moduli(w.vp_obs)
+    ref = orc.cufd(2, lo, mo, ro, w.stf, ids, para, write_files=True, want_gathers=True)["gathers"]
+    ctx = fw.FwiContext(para, 0)
+    got = ctx.obs(lo, mo, ro, w.stf, ids, write_files=False)
+    for a, b in zip(got, ref):
+        assert rel(a, b) < TOL_DATA
+    lam, mu, rho = w.moduli()
+    r1 = orc.cufd(1, lam, mu, rho, w.stf, ids, para)
+    J0 = orc.cufd(0, lam, mu, rho, w.stf, ids, para)["misfit"]
+    J, gl, gm, gd, gs = ctx.misfit_grad(lam, mu, rho, w.stf, ids)
+    assert abs(J - J0) <= TOL_DATA * abs(J0)
+    for k, a in (("g_lambda", gl), ("g_mu", gm), ("g_den", gd), ("g_stf", gs)):
+        assert rel(a, r1[k]) < TOL_GRAD, k
+    ctx.close()
+
+
+def test_cuda_repeatable_and_deterministic(gpu_lib, fw, tmp_path):
+    """No atomics on the imaging path: two runs give identical bits."""
+    from fwiflow_gb300 import synthetic
+
+    w = synthetic.tiny(nz=40, nx=64, nPml=10, nSteps=150, n_shots=2)
+    para = w.write_files(str(tmp_path))
+    ctx = fw.FwiContext(para, 0)
+    ctx.obs(*w.moduli(w.vp_obs), w.stf, [0, 1], write_files=True)
+    a = ctx.misfit_grad(*w.moduli(), w.stf, [0, 1])
+    b = ctx.misfit_grad(*w.moduli(), w.stf, [0, 1])
+    assert a[0] == b[0]
+    for x, y in zip(a[1:], b[1:]):
+        assert np.array_equal(x, y)
+    ctx.close()

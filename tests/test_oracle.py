@@ -1,0 +1,109 @@
+"""The CPU oracle against the reference itself.
+
+* Golden fixtures of tests/golden/ were produced by the reference's own
+  sources (host build, tests/golden/make_golden.py); the oracle must reproduce
+  them to float rounding.
+* Where the host build of the reference is present (oracle/_ref/), the oracle
+  is also compared with it directly on extra geometries.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden_workload, rel
+
+TINY = ["tiny_elastic", "tiny_acoustic", "tiny_window"]
+# Oracle vs reference: both are float programs with the same operation order
+# except the mu / rho scatter (atomicAdd in the reference, a gather here).
+TOL_EXACT = 1e-6
+
+
+@pytest.mark.parametrize("name", TINY)
+def test_oracle_matches_golden(name, orc, tmp_path, fw):
+    d, w, para, moduli = golden_workload(name, tmp_path)
+    ids = list(range(len(w.shots)))
+    lo, mo, ro = moduli(w.vp_obs)
+    r2 = orc.cufd(2, lo, mo, ro, w.stf, ids, para, write_files=True, want_gathers=True)
+    assert rel(np.stack(r2["gathers"]), d["gathers"]) < TOL_EXACT
+    lam, mu, rho = moduli(w.vp)
+    r0 = orc.cufd(0, lam, mu, rho, w.stf, ids, para)
+    assert abs(r0["misfit"] - float(d["misfit"])) <= 1e-6 * abs(float(d["misfit"]))
+    r1 = orc.cufd(1, lam, mu, rho, w.stf, ids, para)
+    for k in ("g_lambda", "g_mu", "g_den", "g_stf"):
+        assert rel(r1[k], d[k]) < TOL_EXACT, k
+
+
+def test_oracle_matches_golden_small_layered(orc, tmp_path, fw):
+    d, w, para, moduli = golden_workload("small_layered", tmp_path)
+    ids = [0, 1]
+    lo, mo, ro = w.moduli(w.vp_obs)
+    r2 = orc.cufd(2, lo, mo, ro, w.stf, ids, para, write_files=True, want_gathers=True)
+    g = np.stack(r2["gathers"])
+    s = int(d["stride"])
+    assert rel(g.reshape(-1)[::s], d["gathers_sub"]) < TOL_EXACT
+    lam, mu, rho = w.moduli()
+    r0 = orc.cufd(0, lam, mu, rho, w.stf, ids, para)
+    assert abs(r0["misfit"] - float(d["misfit"])) <= 1e-6 * abs(float(d["misfit"]))
+    r1 = orc.cufd(1, lam, mu, rho, w.stf, ids, para)
+    for k in ("g_lambda", "g_mu", "g_den"):
+        assert rel(r1[k].reshape(-1)[::s], d[k + "_sub"]) < TOL_EXACT, k
+    assert rel(r1["g_stf"], d["g_stf"]) < TOL_EXACT
+
+
+def test_self_consistency_zero_misfit(orc, tmp_path, fw):
+    """Known answer of docs/src/tutorials/fwi.md:83-87: the misfit of the model
+    that generated the observed data is 0."""
+    from fwiflow_gb300 import synthetic
+
+    w = synthetic.tiny(nz=24, nx=36, nPml=8, nSteps=150, n_shots=1)
+    para = w.write_files(str(tmp_path))
+    lam, mu, rho = w.moduli(w.vp_obs)
+    orc.cufd(2, lam, mu, rho, w.stf, [0], para)
+    assert orc.cufd(0, lam, mu, rho, w.stf, [0], para)["misfit"] == 0.0
+
+
+def _refhost_or_skip(orc):
+    if not orc.refhost_available():
+        pytest.skip("host build of the reference not present (needs the FwiFlow.jl sources at build time)")
+
+
+@pytest.mark.parametrize("case", [
+    dict(nz=20, nx=33, nPml=6, nSteps=120, n_shots=1, seed=3),   # odd nx (launch rounding), thin PML
+    dict(nz=30, nx=26, nPml=9, nSteps=90, n_shots=3, seed=4),    # more shots than columns / 10
+])
+def test_oracle_matches_reference_host_build(case, orc, tmp_path, fw):
+    _refhost_or_skip(orc)
+    from fwiflow_gb300 import synthetic
+
+    w = synthetic.tiny(**case)
+    # Receivers at irregular depths, one duplicated cell.
+    for s in w.shots:
+        s["z_rec"] = [2 + (k % 5) for k in range(len(s["x_rec"]))]
+        s["x_rec"][1] = s["x_rec"][0]
+        s["z_rec"][1] = s["z_rec"][0]
+    para = w.write_files(str(tmp_path))
+    ids = list(range(len(w.shots)))
+    lo, mo, ro = w.moduli(w.vp_obs)
+    a = orc.cufd(2, lo, mo, ro, w.stf, ids, para, write_files=False, want_gathers=True)
+    b = orc.refhost_cufd(2, lo, mo, ro, w.stf, ids, para)  # writes the Data files
+    assert rel(np.concatenate(a["gathers"]), np.concatenate(b["gathers"])) < TOL_EXACT
+    lam, mu, rho = w.moduli()
+    a = orc.cufd(1, lam, mu, rho, w.stf, ids, para)
+    b = orc.refhost_cufd(1, lam, mu, rho, w.stf, ids, para)
+    for k in ("g_lambda", "g_mu", "g_den", "g_stf"):
+        assert rel(a[k], b[k]) < TOL_EXACT, k
+    a = orc.cufd(0, lam, mu, rho, w.stf, ids, para)["misfit"]
+    b = orc.refhost_cufd(0, lam, mu, rho, w.stf, ids, para)["misfit"]
+    assert abs(a - b) <= 1e-6 * abs(b)
+
+
+def test_oracle_rejects_courant_violation(orc, tmp_path, fw):
+    from fwiflow_gb300 import synthetic
+
+    w = synthetic.tiny(nz=24, nx=36, nPml=8, nSteps=50, n_shots=1)
+    w.dt = 0.02  # 10x the stable step
+    para = w.write_files(str(tmp_path))
+    lam, mu, rho = w.moduli()
+    with pytest.raises(RuntimeError, match="status 3"):
+        orc.cufd(2, lam, mu, rho, w.stf, [0], para, write_files=False)
