@@ -155,7 +155,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dipping_grf", choices=["dipping_grf", "small_layered"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-steps", type=int, default=200)
+    ap.add_argument("--cpu-sample-steps", type=int, default=3000)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))

@@ -36,9 +36,20 @@
 
 namespace {
 
+// The reference promotes some products of its time loop to double (a double
+// literal 2.0, MEGA or RSXXZZ in a float expression). prom_t is that type;
+// building with -DORACLE_FP32 makes it float, which gives the same algorithm
+// with FP32 arithmetic only: the tests use it to measure how far FP32 rounding
+// alone moves a result from the reference's (the "FP32 floor" of a case).
+#ifdef ORACLE_FP32
+typedef float prom_t;
+#else
+typedef double prom_t;
+#endif
 constexpr double kPI = 3.141592653589793238462643383279502884197169;  // utilities.h:15
-constexpr double kMEGA = 1e6;                                          // utilities.h:16
-constexpr double kRSXXZZ = 3.0;                                        // utilities.h:21
+constexpr prom_t kMEGA = 1e6;                                          // utilities.h:16
+constexpr prom_t kRSXXZZ = 3.0;                                        // utilities.h:21
+constexpr prom_t kTwo = 2.0;
 constexpr int kLayerStore = 5;                                         // Boundary.cu:24
 
 struct Grid {
@@ -159,8 +170,8 @@ void stress_forward(const Grid& g, const Media& m, const Cpml& c, Fields& f) {
         dvx_dx = dvx_dx / c.K_x[x] + f.m_dvx_dx[i];
       }
       const float lam = m.lam[i], mu = m.mu[i];
-      f.szz[i] = static_cast<float>(f.szz[i] + ((lam + 2.0 * mu) * dvz_dz + lam * dvx_dx) * dt);
-      f.sxx[i] = static_cast<float>(f.sxx[i] + (lam * dvz_dz + (lam + 2.0 * mu) * dvx_dx) * dt);
+      f.szz[i] = static_cast<float>(f.szz[i] + ((lam + kTwo * mu) * dvz_dz + lam * dvx_dx) * dt);
+      f.sxx[i] = static_cast<float>(f.sxx[i] + (lam * dvz_dz + (lam + kTwo * mu) * dvx_dx) * dt);
       float dvx_dz = (C1 * (vx[i + 1] - vx[i]) - C2 * (vx[i + 2] - vx[i - 1])) / dz;
       float dvz_dx = (C1 * (vz[i + nz] - vz[i]) - C2 * (vz[i + 2 * nz] - vz[i - nz])) / dx;
       if (zpml) {
@@ -240,8 +251,8 @@ void velocity_reverse(const Grid& g, const Media& m, Fields& f, std::vector<floa
       const float dsxx_dx = (C1 * (sxx[i + nz] - sxx[i]) - C2 * (sxx[i + 2 * nz] - sxx[i - nz])) / dx;
       f.vx[i] -= (dsxz_dz + dsxx_dx) * m.bycB[i] * dt;
       const float ba = m.bycA[i], bb = m.bycB[i];
-      tA[i] = static_cast<float>(-f.vz_a[i] * (dszz_dz + dsxz_dx) * dt * (-(static_cast<double>(ba) * ba) / 2.0));
-      tB[i] = static_cast<float>(-f.vx_a[i] * (dsxz_dz + dsxx_dx) * dt * (-(static_cast<double>(bb) * bb) / 2.0));
+      tA[i] = static_cast<float>(-f.vz_a[i] * (dszz_dz + dsxz_dx) * dt * (-(static_cast<prom_t>(ba) * ba) / kTwo));
+      tB[i] = static_cast<float>(-f.vx_a[i] * (dsxz_dz + dsxx_dx) * dt * (-(static_cast<prom_t>(bb) * bb) / kTwo));
     }
   }
   // Gather: rho(z,x) receives A and B of (z,x), A of (z-1,x) when z <= z1, and
@@ -280,16 +291,17 @@ void stress_reverse(const Grid& g, const Media& m, Fields& f, std::vector<float>
       const float dvz_dz = (C1 * (vz[i] - vz[i - 1]) - C2 * (vz[i + 1] - vz[i - 2])) / dz;
       const float dvx_dx = (C1 * (vx[i] - vx[i - nz]) - C2 * (vx[i + nz] - vx[i - 2 * nz])) / dx;
       const float lam = m.lam[i], mu = m.mu[i];
-      f.szz[i] = static_cast<float>(f.szz[i] - ((lam + 2.0 * mu) * dvz_dz + lam * dvx_dx) * dt);
-      f.sxx[i] = static_cast<float>(f.sxx[i] - (lam * dvz_dz + (lam + 2.0 * mu) * dvx_dx) * dt);
+      f.szz[i] = static_cast<float>(f.szz[i] - ((lam + kTwo * mu) * dvz_dz + lam * dvx_dx) * dt);
+      f.sxx[i] = static_cast<float>(f.sxx[i] - (lam * dvz_dz + (lam + kTwo * mu) * dvx_dx) * dt);
       const float dvx_dz = (C1 * (vx[i + 1] - vx[i]) - C2 * (vx[i + 2] - vx[i - 1])) / dz;
       const float dvz_dx = (C1 * (vz[i + nz] - vz[i]) - C2 * (vz[i + 2 * nz] - vz[i - nz])) / dx;
       f.sxz[i] -= m.aveMu[i] * (dvx_dz + dvz_dx) * dt;
       gLam[i] = static_cast<float>(gLam[i] + -(f.szz_a[i] + f.sxx_a[i]) * (dvz_dz + dvx_dx) * dt * kMEGA);
-      gMu[i] = static_cast<float>(gMu[i] + (-2.0 * f.szz_a[i] * dvz_dz * dt - 2.0 * f.sxx_a[i] * dvx_dx * dt) * kMEGA);
+      gMu[i] = static_cast<float>(gMu[i] + (-kTwo * f.szz_a[i] * dvz_dz * dt - kTwo * f.sxx_a[i] * dvx_dx * dt) * kMEGA);
       float scale = 0.0f;
       if (m.aveMu[i] != 0.0f) {
-        const double inv_sum = 1.0 / m.mu[i] + 1.0 / m.mu[i + 1] + 1.0 / m.mu[i + nz] + 1.0 / m.mu[i + nz + 1];
+        const prom_t one = 1.0;
+        const prom_t inv_sum = one / m.mu[i] + one / m.mu[i + 1] + one / m.mu[i + nz] + one / m.mu[i + nz + 1];
         scale = static_cast<float>(-f.sxz_a[i] * (dvx_dz + dvz_dx) * dt * m.aveMu[i] / inv_sum * kMEGA);
       }
       tS[i] = scale;
@@ -302,7 +314,7 @@ void stress_reverse(const Grid& g, const Media& m, Fields& f, std::vector<float>
   for (int x = x0; x <= x1 + 1; ++x) {
     for (int z = z0; z <= z1 + 1; ++z) {
       const size_t i = g.at(z, x);
-      const double w = 1.0 / (static_cast<double>(m.mu[i]) * m.mu[i]);
+      const prom_t w = prom_t(1.0) / (static_cast<prom_t>(m.mu[i]) * m.mu[i]);
       float acc = gMu[i];
       bool any = false;
       if (x <= x1 && z <= z1 && m.aveMu[i] != 0.0f) {
@@ -351,7 +363,7 @@ void velocity_adjoint(const Grid& g, const Media& m, const Cpml& c, Fields& f) {
       const float dsxz_dz = (-C1 * (sxz[i] - sxz[i - 1]) + C2 * (sxz[i + 1] - sxz[i - 2])) / dz;
       {
         const float t1 = c.a_x[x] * dpsixx_dx + lam * dszz_dx / c.K_x[x] * dt;
-        const double t = t1 + (lam + 2.0 * mu) * dsxx_dx / c.K_x[x] * dt + c.a_z_half[z] * dpsixz_dz +
+        const prom_t t = t1 + (lam + kTwo * mu) * dsxx_dx / c.K_x[x] * dt + c.a_z_half[z] * dpsixz_dz +
                          m.aveMu[i] / c.K_z_half[z] * dsxz_dz * dt;
         f.vx_a[i] = static_cast<float>(f.vx_a[i] + t);
       }
@@ -363,7 +375,7 @@ void velocity_adjoint(const Grid& g, const Media& m, const Cpml& c, Fields& f) {
       const float dpsizx_dx = (-C1 * (mvzx[i] - mvzx[i - nz]) + C2 * (mvzx[i + nz] - mvzx[i - 2 * nz])) / dx;
       const float dsxz_dx = (-C1 * (sxz[i] - sxz[i - nz]) + C2 * (sxz[i + nz] - sxz[i - 2 * nz])) / dx;
       {
-        const double t = c.a_z[z] * dpsizz_dz + (lam + 2.0 * mu) * dszz_dz / c.K_z[z] * dt +
+        const prom_t t = c.a_z[z] * dpsizz_dz + (lam + kTwo * mu) * dszz_dz / c.K_z[z] * dt +
                          lam * dsxx_dz / c.K_z[z] * dt + c.a_x_half[x] * dpsizx_dx +
                          m.aveMu[i] / c.K_x_half[x] * dsxz_dx * dt;
         f.vz_a[i] = static_cast<float>(f.vz_a[i] + t);
@@ -405,8 +417,8 @@ void stress_adjoint(const Grid& g, const Media& m, const Cpml& c, Fields& f) {
       f.sxx_a[i] += c.a_x_half[x] * dphi_xx_x_dx + m.bycB[i] * dvx_dx / c.K_x_half[x] * dt;
       f.szz_a[i] += c.a_z_half[z] * dphi_zz_z_dz + m.bycA[i] * dvz_dz / c.K_z_half[z] * dt;
       f.m_dvx_dx[i] = static_cast<float>(c.b_x[x] * f.m_dvx_dx[i] + lam * f.szz_a[i] * dt +
-                                         (lam + 2.0 * mu) * f.sxx_a[i] * dt);
-      f.m_dvz_dz[i] = static_cast<float>(c.b_z[z] * f.m_dvz_dz[i] + (lam + 2.0 * mu) * f.szz_a[i] * dt +
+                                         (lam + kTwo * mu) * f.sxx_a[i] * dt);
+      f.m_dvz_dz[i] = static_cast<float>(c.b_z[z] * f.m_dvz_dz[i] + (lam + kTwo * mu) * f.szz_a[i] * dt +
                                          lam * f.sxx_a[i] * dt);
     }
   }
@@ -421,7 +433,7 @@ void add_source(const Grid& g, Fields& f, float amp, int zs, int xs, bool isFor,
       const size_t i = g.at(zs + gz - 4, xs + gx - 4);
       const float ga = gauss[gz + gx * 9];
       const float t = scale * amp * g.dt * ga;
-      const double t3 = kRSXXZZ * scale * amp * g.dt * ga;
+      const prom_t t3 = kRSXXZZ * scale * amp * g.dt * ga;
       if (isFor) {
         f.szz[i] += t;
         f.sxx[i] = static_cast<float>(f.sxx[i] + t3);
@@ -585,8 +597,8 @@ int oracle_cufd(const oracle_para* p, const oracle_shot* shots, int group_size, 
   m.den.resize(n);
   for (int z = 0; z < nz; ++z)
     for (int x = 0; x < nx; ++x) {
-      m.lam[g.at(z, x)] = static_cast<float>(Lambda[static_cast<size_t>(z) * nx + x] * kMEGA);
-      m.mu[g.at(z, x)] = static_cast<float>(Mu[static_cast<size_t>(z) * nx + x] * kMEGA);
+      m.lam[g.at(z, x)] = static_cast<float>(Lambda[static_cast<size_t>(z) * nx + x] * 1e6);
+      m.mu[g.at(z, x)] = static_cast<float>(Mu[static_cast<size_t>(z) * nx + x] * 1e6);
       m.den[g.at(z, x)] = static_cast<float>(Den[static_cast<size_t>(z) * nx + x]);
     }
   m.aveMu.assign(n, 0.0f);

@@ -22,6 +22,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "liboracle_fwi.so")
+# Same algorithm built with FP32 arithmetic only (-DORACLE_FP32): its distance
+# from the reference is the rounding floor of FP32 for a given case.
+ORACLE_FP32_LIB = os.path.join(HERE, "_build", "liboracle_fwi_fp32.so")
 REFHOST_LIB = os.path.join(HERE, "_ref", "librefhost_fwi.so")
 
 
@@ -38,19 +41,19 @@ class _Shot(ctypes.Structure):
                 ("weights", ctypes.POINTER(ctypes.c_float))]
 
 
-_oracle = None
+_oracles = {}
 _refhost = None
 
 
-def _load_oracle():
-    global _oracle
-    if _oracle is None:
-        if not os.path.exists(ORACLE_LIB):
-            raise RuntimeError(f"oracle library not built: {ORACLE_LIB} (run make -C oracle)")
-        lib = ctypes.CDLL(ORACLE_LIB)
+def _load_oracle(precision: str = "reference"):
+    if precision not in _oracles:
+        path = ORACLE_LIB if precision == "reference" else ORACLE_FP32_LIB
+        if not os.path.exists(path):
+            raise RuntimeError(f"oracle library not built: {path} (run make -C oracle)")
+        lib = ctypes.CDLL(path)
         lib.oracle_cufd.restype = ctypes.c_int
-        _oracle = lib
-    return _oracle
+        _oracles[precision] = lib
+    return _oracles[precision]
 
 
 def refhost_available() -> bool:
@@ -118,7 +121,8 @@ def _iptr(a):
 
 
 def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads: int = 0,
-         obs: Optional[Sequence[np.ndarray]] = None, write_files: bool = True, want_gathers: bool = False) -> dict:
+         obs: Optional[Sequence[np.ndarray]] = None, write_files: bool = True, want_gathers: bool = False,
+         precision: str = "reference") -> dict:
     """Oracle run of one `cufd` call (libCUFD.cu:34-580).
 
     lam, mu [MPa] and den are row-major float64 [nz][nx]; stf is
@@ -126,6 +130,7 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
     are read from `data_dir_name/Shot<id>.bin` unless `obs` is given; for
     calc_id 2 the gathers are written there when `write_files`.
     Returns misfit, g_lambda, g_mu, g_den, g_stf and (optionally) gathers.
+    precision "fp32" runs the FP32-only build (no double promotions).
     """
     p = load_para(para_fname)
     shot_ids = [int(v) for v in np.asarray(shot_ids).ravel()]
@@ -171,7 +176,7 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
     g_den = np.zeros((nz, nx))
     g_stf = np.zeros_like(stf)
     ids = np.asarray(shot_ids, dtype=np.int32)
-    rc = _load_oracle().oracle_cufd(
+    rc = _load_oracle(precision).oracle_cufd(
         ctypes.byref(para), carr, n, _iptr(ids), _dptr(lam), _dptr(mu), _dptr(den), _dptr(stf), int(calc_id),
         obs_ptrs, syn_ptrs, None, ctypes.byref(misfit), _dptr(g_lam), _dptr(g_mu), _dptr(g_den), _dptr(g_stf),
         int(nthreads))

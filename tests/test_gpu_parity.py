@@ -15,26 +15,45 @@ TOL_DATA = 1e-4
 TOL_GRAD = 1e-3
 
 
+def fp32_floor(orc, w, para, moduli, ids, d):
+    """Distance from the reference of the reference's own algorithm evaluated
+    with FP32 arithmetic only (oracle built with -DORACLE_FP32). It is the
+    rounding floor of the case: a well-conditioned elastic case sits near 1e-6,
+    an acoustic one (Vs = 0) much higher, because the deviatoric stress the
+    source injects never radiates and the trace recorded on the source cell
+    is a large static value minus a small residual."""
+    lo, mo, ro = moduli(w.vp_obs)
+    g = orc.cufd(2, lo, mo, ro, w.stf, ids, para, write_files=False, want_gathers=True, precision="fp32")
+    lam, mu, rho = moduli(w.vp)
+    obs = list(d["gathers"])
+    r1 = orc.cufd(1, lam, mu, rho, w.stf, ids, para, obs=obs, precision="fp32")
+    J = orc.cufd(0, lam, mu, rho, w.stf, ids, para, obs=obs, precision="fp32")["misfit"]
+    out = {k: rel(r1[k], d[k]) for k in ("g_lambda", "g_mu", "g_den", "g_stf")}
+    out["gathers"] = rel(np.stack(g["gathers"]), d["gathers"])
+    out["misfit"] = abs(J - float(d["misfit"])) / abs(float(d["misfit"]))
+    return out
+
+
 @pytest.mark.parametrize("name", ["tiny_elastic", "tiny_acoustic", "tiny_window"])
-def test_cuda_matches_reference_golden(name, gpu_lib, fw, tmp_path):
+def test_cuda_matches_reference_golden(name, gpu_lib, fw, orc, tmp_path):
+    """Tolerance: 1e-4 (data, misfit) / 1e-3 (gradients), or 4x the case's FP32
+    floor where FP32 rounding alone already moves the reference further."""
     d, w, para, moduli = golden_workload(name, tmp_path)
     ids = list(range(len(w.shots)))
+    floor = fp32_floor(orc, w, para, moduli, ids, d)
+    tol = {k: max(TOL_DATA if k in ("gathers", "misfit") else TOL_GRAD, 4.0 * v) for k, v in floor.items()}
     ctx = fw.FwiContext(para, 0)
     lo, mo, ro = moduli(w.vp_obs)
-    g = ctx.obs(lo, mo, ro, w.stf, ids, write_files=True)
-    assert rel(np.stack(g), d["gathers"]) < TOL_DATA
+    g = ctx.obs(lo, mo, ro, w.stf, ids, write_files=False)
+    assert rel(np.stack(g), d["gathers"]) < tol["gathers"]
     lam, mu, rho = moduli(w.vp)
-    J = ctx.misfit(lam, mu, rho, w.stf, ids)
-    assert abs(J - float(d["misfit"])) <= TOL_DATA * abs(float(d["misfit"]))
-    J2, gl, gm, gd, gs = ctx.misfit_grad(lam, mu, rho, w.stf, ids)
+    obs = list(d["gathers"])
+    J = ctx.misfit(lam, mu, rho, w.stf, ids, obs=obs)
+    assert abs(J - float(d["misfit"])) <= tol["misfit"] * abs(float(d["misfit"]))
+    J2, gl, gm, gd, gs = ctx.misfit_grad(lam, mu, rho, w.stf, ids, obs=obs)
     assert abs(J2 - J) <= 1e-6 * abs(J)  # one forward pass gives the same misfit
-    assert rel(gl, d["g_lambda"]) < TOL_GRAD
-    assert rel(gd, d["g_den"]) < TOL_GRAD
-    assert rel(gs, d["g_stf"]) < TOL_GRAD
-    if name == "tiny_acoustic":
-        assert np.abs(gm).max() == 0.0 or rel(gm, d["g_mu"]) < TOL_GRAD
-    else:
-        assert rel(gm, d["g_mu"]) < TOL_GRAD
+    for k, a in (("g_lambda", gl), ("g_mu", gm), ("g_den", gd), ("g_stf", gs)):
+        assert rel(a, d[k]) < tol[k], (k, rel(a, d[k]), tol[k])
     ctx.close()
 
 
