@@ -49,13 +49,13 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def workload(name):
+def workload(name, nsteps=None):
     fw = ge.load_package()
     from fwiflow_gb300 import synthetic
 
     if name == "small_layered":
-        return synthetic.small_layered()
-    return synthetic.dipping_grf()
+        return synthetic.small_layered(**({"nSteps": nsteps} if nsteps else {}))
+    return synthetic.dipping_grf(**({"nSteps": nsteps} if nsteps else {}))
 
 
 def describe(w):
@@ -156,12 +156,14 @@ def main():
     ap.add_argument("--workload", default="dipping_grf", choices=["dipping_grf", "small_layered"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-steps", type=int, default=3000)
+    ap.add_argument("--nsteps", type=int, default=None,
+                    help="override the workload's time steps (small cases for profiler captures)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    w = workload(args.workload)
+    w = workload(args.workload, args.nsteps)
     metric, unit = "fwd+adj Gpts/s vs HBM roofline", "Gpts/s"
     cfg = {"workload": describe(w), "cells": w.cells, "nSteps": w.nSteps, "shots": len(w.shots),
            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
