@@ -146,6 +146,26 @@ int fwigb_set_kernel_timing(fwigb_ctx *ctx, int enable);
  * total_ms[4] and launches[4], indexed by kind. */
 int fwigb_kernel_times(fwigb_ctx *ctx, double *total_ms, long long *launches);
 
+/* ---- Allocation-free misfit (no counterpart in the reference) ----
+ * For callers that cannot call cudaMalloc: an operator inside a framework that
+ * owns the device memory pool (TensorFlow's allocator, as for FwiFlow's own TF
+ * op; an XLA / JAX runtime that reserved the GPU), or a service with a fixed
+ * device-memory budget. Computes what fwigb_misfit computes for one shot from
+ * gathers the caller already holds on the device: d_obs, d_syn and d_res are
+ * device buffers [nrec][nSteps] float with 1 <= nrec <= 65536; d_syn is tapered
+ * in place, d_res receives the adjoint source, *misfit (host) the misfit.
+ * The only scratch is a static device array of 65537 doubles that every GPU
+ * loading the library keeps until exit; all calls share it, so calls that
+ * overlap on the GPU race. The first call on a device (with that device
+ * current) looks up the array's address: make it before any stream capture.
+ * Synchronises `stream` (a cudaStream_t; NULL for the legacy default stream).
+ * Allocates nothing. */
+int fwigb_misfit_gathers_noalloc(const float *d_obs, float *d_syn, float *d_res, int nrec, int nSteps, float dt,
+                                 double *misfit, void *stream);
+
+/* Message of the last failure of fwigb_misfit_gathers_noalloc (thread-local). */
+const char *fwigb_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
