@@ -241,6 +241,7 @@ def main():
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     launches_per_step = ctx.last_launch_count()
+    cfg["tile_widths"] = dict(zip(SWEEP_NAMES, ctx.tile_config()))
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, stops)]
     dev_s = sum(step_ms) / 1e3
     if world > 1:

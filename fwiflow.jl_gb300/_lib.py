@@ -56,6 +56,8 @@ SIGNATURES = {
     "fwigb_stream": ([_V], _V),
     "fwigb_last_launch_count": ([_V], ctypes.c_longlong),
     "fwigb_set_kernel_timing": ([_V, ctypes.c_int], ctypes.c_int),
+    "fwigb_tile_config": ([_V, _I], ctypes.c_int),
+    "fwigb_set_tile_config": ([_V, _I], ctypes.c_int),
     "fwigb_kernel_times": ([_V, _D, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
 }
 

@@ -328,7 +328,12 @@ struct fwigb_ctx {
   int nrec_max = 0;
   Geo geo{};
   cudaStream_t stream = nullptr;
-  size_t cells = 0;
+  size_t cells = 0;   // allocated cells per grid array (ldz * nx)
+  size_t ncell = 0;   // logical cells (nz * nx), the size of host arrays
+  SweepMaps maps[3];  // tensor maps for tile widths 8, 16, 32
+  int tx[4] = {16, 16, 16, 16};  // tile width per sweep (F1, F2, B, C)
+  bool tuned_fwd = false, tuned_bwd = false;
+  bool autotune = true;
   // device buffers
   DevBuf media, stage, cpml, fields, grads, store, scal, partials;
   DevBuf shot_src, shot_rec, shot_blk, shot_data, shot_taper, shot_gstf;
@@ -336,7 +341,8 @@ struct fwigb_ctx {
   std::vector<StagedShot> staged;
   bool with_obs = false;
   bool per_trace_taper = false;
-  int nblk = 0;
+  int nblk = 0;  // receiver bins (32 x 8 cells)
+  int nbin_z = 0;
   bool model_set = false;
   int last_calc = -1;
   long long launches = 0;
@@ -350,6 +356,12 @@ namespace {
 
 thread_local std::string g_err;
 
+#define TRY_RC(call)                  \
+  do {                                \
+    int rc_ = (call);                 \
+    if (rc_ != FWIGB_OK) return rc_;  \
+  } while (0)
+
 #define CK(call)                                                                                   \
   do {                                                                                             \
     cudaError_t e_ = (call);                                                                       \
@@ -358,6 +370,8 @@ thread_local std::string g_err;
       return (e_ == cudaErrorMemoryAllocation) ? FWIGB_ERR_OOM : FWIGB_ERR_CUDA;                   \
     }                                                                                              \
   } while (0)
+
+int tx_slot(int tx) { return tx == 8 ? 0 : (tx == 16 ? 1 : 2); }
 
 Fields fields_of(fwigb_ctx* ctx) {
   float* b = ctx->fields.as<float>();
@@ -410,6 +424,7 @@ int setup_geometry(fwigb_ctx* ctx) {
   Geo& g = ctx->geo;
   g.nz = p.nz;
   g.nx = p.nx;
+  g.ldz = (p.nz + 31) / 32 * 32;
   g.nPml = p.nPml;
   g.nPad = p.nPad;
   g.zs0 = 2;
@@ -433,7 +448,8 @@ int setup_geometry(fwigb_ctx* ctx) {
   g.dt = p.dt;
   g.rdz = 1.0f / p.dz;
   g.rdx = 1.0f / p.dx;
-  ctx->cells = static_cast<size_t>(p.nz) * p.nx;
+  ctx->cells = static_cast<size_t>(g.ldz) * p.nx;
+  ctx->ncell = static_cast<size_t>(p.nz) * p.nx;
 
   // CPML profiles (host) and the adjoint-memory bands derived from them.
   std::vector<float> h(6 * p.nz + 6 * p.nx);
@@ -459,12 +475,26 @@ int setup_geometry(fwigb_ctx* ctx) {
   CK(ctx->cpml.ensure(h.size() * sizeof(float)));
   CK(cudaMemcpy(ctx->cpml.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
   CK(ctx->media.ensure(9 * ctx->cells * sizeof(float)));
-  CK(ctx->stage.ensure(3 * ctx->cells * sizeof(double)));
+  CK(ctx->stage.ensure(3 * ctx->ncell * sizeof(double)));
   CK(ctx->fields.ensure(18 * ctx->cells * sizeof(float)));
   CK(ctx->grads.ensure(3 * ctx->cells * sizeof(float)));
-  CK(ctx->scal.ensure(64));  // [0]: misfit accumulator (double), [8..]: cp max bits
+  // [0]: misfit accumulator (double), [8]: cp max bits, [16]: sweep error word
+  CK(ctx->scal.ensure(64));
+  CK(cudaMemset(ctx->scal.p, 0, 64));
+  // Padding rows (ldz > nz) and every field start at zero.
+  CK(cudaMemset(ctx->media.p, 0, 9 * ctx->cells * sizeof(float)));
+  CK(cudaMemset(ctx->fields.p, 0, 18 * ctx->cells * sizeof(float)));
   CK(ctx->partials.ensure(1024 * sizeof(double)));
-  ctx->nblk = ((p.nz + kTileZ - 1) / kTileZ) * ((p.nx + kTileX - 1) / kTileX);
+  ctx->nbin_z = (p.nz + kBinZ - 1) / kBinZ;
+  ctx->nblk = ctx->nbin_z * ((p.nx + kBinX - 1) / kBinX);
+  const Fields f = fields_of(ctx);
+  for (int k = 0; k < 3; ++k) {
+    const char* why = nullptr;
+    if (!encode_sweep_maps(g, f, kTileXs[k], ctx->maps[k], &why)) {
+      ctx->err = why;
+      return FWIGB_ERR_CUDA;
+    }
+  }
   return FWIGB_OK;
 }
 
@@ -491,17 +521,19 @@ int set_model(fwigb_ctx* ctx, const double* lam, const double* mu, const double*
     return FWIGB_ERR_ARG;
   }
   CK(cudaSetDevice(ctx->device));
-  const size_t n = ctx->cells;
+  const size_t nh = ctx->ncell, n = ctx->cells;
+  const int ldz = ctx->geo.ldz;
   double* st = ctx->stage.as<double>();
-  CK(cudaMemcpyAsync(st, lam, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(st + n, mu, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(st + 2 * n, den, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(st, lam, nh * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(st + nh, mu, nh * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(st + 2 * nh, den, nh * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   unsigned* cpbits = reinterpret_cast<unsigned*>(ctx->scal.as<char>() + 8);
   CK(cudaMemsetAsync(cpbits, 0, sizeof(unsigned), ctx->stream));
   float* b = ctx->media.as<float>();
-  launch_media_from_rowmajor(ctx->stream, ctx->p.nz, ctx->p.nx, st, st + n, st + 2 * n, b, b + n, b + 2 * n, cpbits);
-  launch_media_derived(ctx->stream, ctx->p.nz, ctx->p.nx, b, b + n, b + 2 * n, b + 3 * n, b + 4 * n, b + 5 * n,
-                       b + 6 * n, b + 7 * n, b + 8 * n, cpbits);
+  launch_media_from_rowmajor(ctx->stream, ctx->p.nz, ctx->p.nx, ldz, st, st + nh, st + 2 * nh, b, b + n, b + 2 * n,
+                             cpbits);
+  launch_media_derived(ctx->stream, ctx->p.nz, ctx->p.nx, ldz, b, b + n, b + 2 * n, b + 3 * n, b + 4 * n, b + 5 * n,
+                       b + 6 * n, b + 7 * n, b + 8 * n);
   CK(cudaGetLastError());
   unsigned bits = 0;
   CK(cudaMemcpyAsync(&bits, cpbits, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
@@ -569,7 +601,7 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
   CK(cudaMemcpyAsync(ctx->shot_src.p, hsrc.data(), hsrc.size() * sizeof(float), cudaMemcpyHostToDevice,
                      ctx->stream));
   // Receivers and their per-block lists (CSR over the sweep grid).
-  const int nbz = (p.nz + kTileZ - 1) / kTileZ;
+  const int nbz = ctx->nbin_z;
   const int nblk = ctx->nblk;
   std::vector<int> hrec(2 * ns * nrm, 0), hblk(ns * (nblk + 1 + nrm), 0);
   for (size_t s = 0; s < ns; ++s) {
@@ -583,12 +615,12 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
     for (int r = 0; r < nrec; ++r) {
       rz[r] = g.z_rec[r];
       rx[r] = g.x_rec[r];
-      cnt[(g.z_rec[r] / kTileZ) + (g.x_rec[r] / kTileX) * nbz + 1]++;
+      cnt[(g.z_rec[r] / kBinZ) + (g.x_rec[r] / kBinX) * nbz + 1]++;
     }
     for (int b = 0; b < nblk; ++b) cnt[b + 1] += cnt[b];
     for (int b = 0; b <= nblk; ++b) off[b] = cnt[b];
     std::vector<int> pos(cnt.begin(), cnt.end() - 1);
-    for (int r = 0; r < nrec; ++r) lst[pos[(g.z_rec[r] / kTileZ) + (g.x_rec[r] / kTileX) * nbz]++] = r;
+    for (int r = 0; r < nrec; ++r) lst[pos[(g.z_rec[r] / kBinZ) + (g.x_rec[r] / kBinX) * nbz]++] = r;
   }
   CK(ctx->shot_rec.ensure(hrec.size() * sizeof(int)));
   CK(ctx->shot_blk.ensure(hblk.size() * sizeof(int)));
@@ -652,6 +684,58 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
   return FWIGB_OK;
 }
 
+// Tile-width autotuner: times every width of each sweep on this context's grid
+// (a few launches each on the live buffers, which the run then resets) and
+// keeps the fastest. Forward sweeps are tuned on the first run, backward sweeps
+// on the first run with the adjoint.
+int autotune(fwigb_ctx* ctx, const ShotD& sh, bool adj) {
+  cudaStream_t s = ctx->stream;
+  const Geo& g = ctx->geo;
+  Fields f = fields_of(ctx);
+  MediaD m = media_of(ctx);
+  CpmlD c = cpml_of(ctx);
+  StoreD st{ctx->store.as<float>()};
+  float* gb = ctx->grads.as<float>();
+  Grads gr{gb, gb + ctx->cells, gb + 2 * ctx->cells};
+  unsigned* d_err = reinterpret_cast<unsigned*>(ctx->scal.as<char>() + 16);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int kinds_end = (adj && ctx->p.nSteps >= 2) ? 4 : 2;
+  for (int kind = ctx->tuned_fwd ? 2 : 0; kind < kinds_end; ++kind) {
+    float best = 1e30f;
+    for (int slot = 0; slot < 3; ++slot) {
+      const int tx = kTileXs[slot];
+      const SweepMaps& mp = ctx->maps[slot];
+      auto launch = [&]() {
+        switch (kind) {
+          case 0: launch_fwd_stress(s, tx, mp.f1, g, f, m, c, sh, st, 0, false, d_err); break;
+          case 1: launch_fwd_velocity(s, tx, mp.f2, g, f, m, c, d_err); break;
+          case 2: launch_bwd_B(s, tx, mp.b, g, f, m, c, sh, st, gr, 0, d_err); break;
+          default: launch_bwd_C(s, tx, mp.c, g, f, m, c, sh, st, gr, 1, true, d_err); break;
+        }
+      };
+      for (int w = 0; w < 2; ++w) launch();
+      CK(cudaEventRecord(e0, s));
+      for (int r = 0; r < 10; ++r) launch();
+      CK(cudaEventRecord(e1, s));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0.0f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) {
+        best = ms;
+        ctx->tx[kind] = tx;
+      }
+    }
+  }
+  CK(cudaGetLastError());
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->tuned_fwd = true;
+  if (kinds_end == 4) ctx->tuned_bwd = true;
+  return FWIGB_OK;
+}
+
 int run(fwigb_ctx* ctx, int calc_id) {
   if (calc_id < 0 || calc_id > 2) {
     ctx->err = "calc_id must be 0, 1 or 2";
@@ -680,6 +764,27 @@ int run(fwigb_ctx* ctx, int calc_id) {
   if (adj) {
     const size_t store_bytes = static_cast<size_t>(nt) * 5 * g.ring_len * sizeof(float);
     CK(ctx->store.ensure(store_bytes));
+  }
+  if (ctx->autotune && (!ctx->tuned_fwd || (adj && !ctx->tuned_bwd))) {
+    const StagedShot& S0 = ctx->staged[0];
+    ShotD sh{};
+    sh.src_z = S0.geom->z_src;
+    sh.src_x = S0.geom->x_src;
+    sh.src_szz = ctx->shot_src.as<float>(0);
+    sh.src_sxx = ctx->shot_src.as<float>(nt);
+    sh.nrec = S0.nrec;
+    sh.nSteps = nt;
+    sh.rec_z = ctx->shot_rec.as<int>(0);
+    sh.rec_x = sh.rec_z + nrm;
+    sh.blk_off = ctx->shot_blk.as<int>(0);
+    sh.blk_rec = sh.blk_off + ctx->nblk + 1;
+    sh.nbin_z = ctx->nbin_z;
+    sh.data = ctx->shot_data.as<float>(ns * per);
+    sh.res = ctx->shot_data.as<float>(2 * ns * per);
+    sh.gstf = ctx->shot_gstf.as<float>(0);
+    TRY_RC(autotune(ctx, sh, adj));
+  }
+  if (adj) {
     CK(cudaMemsetAsync(ctx->grads.p, 0, 3 * ctx->cells * sizeof(float), s));
     CK(cudaMemsetAsync(ctx->shot_gstf.p, 0, ns * nt * sizeof(float), s));
   }
@@ -691,6 +796,8 @@ int run(fwigb_ctx* ctx, int calc_id) {
   StoreD st{ctx->store.as<float>()};
   float* gb = ctx->grads.as<float>();
   Grads gr{gb, gb + ctx->cells, gb + 2 * ctx->cells};
+  unsigned* d_err = reinterpret_cast<unsigned*>(ctx->scal.as<char>() + 16);
+  auto mp = [&](int kind) -> const SweepMaps& { return ctx->maps[tx_slot(ctx->tx[kind])]; };
   long long launches = 0;
   ctx->ev_kind.clear();
   size_t ev_used = 0;
@@ -727,6 +834,7 @@ int run(fwigb_ctx* ctx, int calc_id) {
     sh.rec_x = sh.rec_z + nrm;
     sh.blk_off = ctx->shot_blk.as<int>(is * (ctx->nblk + 1 + nrm));
     sh.blk_rec = sh.blk_off + ctx->nblk + 1;
+    sh.nbin_z = ctx->nbin_z;
     float* d_obs = ctx->shot_data.as<float>(is * per);
     float* d_syn = ctx->shot_data.as<float>((ns + is) * per);
     float* d_res = ctx->shot_data.as<float>((2 * ns + is) * per);
@@ -737,8 +845,8 @@ int run(fwigb_ctx* ctx, int calc_id) {
     CK(cudaMemsetAsync(ctx->fields.p, 0, 18 * ctx->cells * sizeof(float), s));
     CK(cudaMemsetAsync(d_syn, 0, per * sizeof(float), s));
     for (int it = 0; it <= nt - 2; ++it) {
-      TIMED(0, launch_fwd_stress(s, g, f, m, c, sh, st, it, adj));
-      TIMED(1, launch_fwd_velocity(s, g, f, m, c));
+      TIMED(0, launch_fwd_stress(s, ctx->tx[0], mp(0).f1, g, f, m, c, sh, st, it, adj, d_err));
+      TIMED(1, launch_fwd_velocity(s, ctx->tx[1], mp(1).f2, g, f, m, c, d_err));
       launches += 2;
     }
     if (if_res) {
@@ -757,11 +865,11 @@ int run(fwigb_ctx* ctx, int calc_id) {
       // The reference's first el_velocity_adj acts on all-zero fields (no-op);
       // then res_injection(nSteps-1) + el_stress_adj, source_grad(nSteps-2),
       // reverse velocity of step nSteps-2 ... (libCUFD.cu:353-445).
-      TIMED(3, launch_bwd_C(s, g, f, m, c, sh, st, gr, nt - 1, nt - 1 >= 1));
+      TIMED(3, launch_bwd_C(s, ctx->tx[3], mp(3).c, g, f, m, c, sh, st, gr, nt - 1, nt - 1 >= 1, d_err));
       ++launches;
       for (int it = nt - 2; it >= 0; --it) {
-        TIMED(2, launch_bwd_B(s, g, f, m, c, sh, st, gr, it));
-        TIMED(3, launch_bwd_C(s, g, f, m, c, sh, st, gr, it, it >= 1));
+        TIMED(2, launch_bwd_B(s, ctx->tx[2], mp(2).b, g, f, m, c, sh, st, gr, it, d_err));
+        TIMED(3, launch_bwd_C(s, ctx->tx[3], mp(3).c, g, f, m, c, sh, st, gr, it, it >= 1, d_err));
         launches += 2;
       }
     }
@@ -797,6 +905,16 @@ int fetch(fwigb_ctx* ctx, double* misfit, double* g_lam, double* g_mu, double* g
   const size_t ns = ctx->staged.size();
   const int nt = p.nSteps;
   const size_t per = static_cast<size_t>(ctx->nrec_max) * nt;
+  {
+    unsigned e = 0;
+    CK(cudaMemcpyAsync(&e, ctx->scal.as<char>() + 16, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (e) {
+      CK(cudaMemsetAsync(ctx->scal.as<char>() + 16, 0, sizeof(unsigned), s));
+      ctx->err = "a sweep gave up waiting for its staged tiles (bounded wait); results are invalid";
+      return FWIGB_ERR_TIMEOUT;
+    }
+  }
   if (misfit) {
     double acc = 0.0;
     CK(cudaMemcpyAsync(&acc, ctx->scal.p, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -810,10 +928,11 @@ int fetch(fwigb_ctx* ctx, double* misfit, double* g_lam, double* g_mu, double* g
     }
     double* out[3] = {g_lam, g_mu, g_den};
     double* st = ctx->stage.as<double>();
+    const size_t nh = ctx->ncell;
     for (int k = 0; k < 3; ++k) {
       if (!out[k]) continue;
-      launch_to_rowmajor(s, p.nz, p.nx, ctx->grads.as<float>(k * n), st + k * n, 1.0);
-      CK(cudaMemcpyAsync(out[k], st + k * n, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+      launch_to_rowmajor(s, p.nz, p.nx, ctx->geo.ldz, ctx->grads.as<float>(k * n), st + k * nh, 1.0);
+      CK(cudaMemcpyAsync(out[k], st + k * nh, nh * sizeof(double), cudaMemcpyDeviceToHost, s));
     }
   }
   if (g_stf) {
@@ -956,6 +1075,30 @@ int fwigb_synchronize(fwigb_ctx* ctx) {
 void* fwigb_stream(fwigb_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
 
 long long fwigb_last_launch_count(const fwigb_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int fwigb_tile_config(const fwigb_ctx* ctx, int* tile_x) {
+  if (!ctx || !tile_x) return FWIGB_ERR_ARG;
+  for (int k = 0; k < 4; ++k) tile_x[k] = ctx->tx[k];
+  return FWIGB_OK;
+}
+
+int fwigb_set_tile_config(fwigb_ctx* ctx, const int* tile_x) {
+  if (!ctx) return FWIGB_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!tile_x) {
+    ctx->autotune = true;
+    ctx->tuned_fwd = ctx->tuned_bwd = false;
+    return FWIGB_OK;
+  }
+  for (int k = 0; k < 4; ++k)
+    if (tile_x[k] != 8 && tile_x[k] != 16 && tile_x[k] != 32) {
+      ctx->err = "tile widths must be 8, 16 or 32";
+      return FWIGB_ERR_ARG;
+    }
+  for (int k = 0; k < 4; ++k) ctx->tx[k] = tile_x[k];
+  ctx->autotune = false;
+  return FWIGB_OK;
+}
 
 int fwigb_set_kernel_timing(fwigb_ctx* ctx, int enable) {
   if (!ctx) return FWIGB_ERR_ARG;

@@ -1,24 +1,41 @@
 // Device-side data structures of the GB300 elastic FWI engine and the host
 // launch interface of its kernels (implemented in kernels.cu).
 //
-// Layout in HBM: every grid array is column-major [nx][nz] float, z fastest,
-// as in the reference (a(z,x) = a[x*nz + z], el_stress.cu:1-19), so one warp
-// reads 32 consecutive depths of one column in a single 128-byte transaction.
+// Layout in HBM: every grid array is column-major [nx][ldz] float, z fastest,
+// as in the reference (a(z,x) = a[x*nz + z], el_stress.cu:1-19) but with the
+// column stride ldz = nz rounded up to 32, so every column starts on a
+// 128-byte boundary: one warp reads 32 consecutive depths in one transaction
+// and every TMA tile of the sweeps starts 16-byte aligned.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
 
 namespace fwigb {
 
-// Thread-block tile of the grid sweeps: 32 depths (one warp) x kTileX columns.
+// Sweep tiles: 32 depths (one per lane) x TX columns, TX in {8, 16, 32}
+// (chosen per sweep by the autotuner); 4 warps per block.
 constexpr int kTileZ = 32;
-constexpr int kTileX = 8;
+constexpr int kSweepThreads = 128;
+// Receivers are binned on a fixed 32 x 8 grid, independent of the sweep tile.
+constexpr int kBinZ = 32;
+constexpr int kBinX = 8;
+// TMA box of one staged array: depths z0-4 .. z0+35 (start aligned to 16
+// bytes), columns x0-2 .. x0+TX+1.
+constexpr int kBoxZ = kTileZ + 8;
+constexpr int kTileXs[3] = {8, 16, 32};
+
+// Tensor maps of the (up to 5) arrays a sweep stages into shared memory.
+struct alignas(64) TileMaps {
+  CUtensorMap t[5];
+};
 
 // Grid geometry and the index ranges of the reference kernels.
 struct Geo {
   int nz, nx, nPml, nPad;
+  int ldz;                 // column stride of every grid array (nz rounded up to 32)
   int zs0, zs1, xs0, xs1;  // stencil domain [2, nz-nPad-3] x [2, nx-3] (el_stress.cu:52)
   int zi0, zi1, xi0, xi1;  // reverse-time interior (el_stress.cu:93)
   int zpml_hi;             // z-PML: z < nPml || z > zpml_hi   (= nz-nPml-nPad-1)
@@ -62,8 +79,9 @@ struct ShotD {
   int nrec, nSteps;
   const int* rec_z;       // receiver cells
   const int* rec_x;
-  const int* blk_off;     // receivers per thread block (CSR over the sweep grid)
+  const int* blk_off;     // receivers per 32 x 8 bin (CSR over the bins)
   const int* blk_rec;
+  int nbin_z;             // bins along z
   float* data;            // synthetic gathers [nrec][nSteps]
   const float* res;       // adjoint source [nrec][nSteps]
   float* gstf;            // source-time-function gradient [nSteps]
@@ -79,22 +97,35 @@ struct Grads {
   float* den;
 };
 
-// ---- launchers (kernels.cu) ----
-void launch_fwd_stress(cudaStream_t s, const Geo& g, const Fields& f, const MediaD& m, const CpmlD& c,
-                       const ShotD& sh, const StoreD& st, int it, bool save);
-void launch_fwd_velocity(cudaStream_t s, const Geo& g, const Fields& f, const MediaD& m, const CpmlD& c);
-void launch_bwd_B(cudaStream_t s, const Geo& g, const Fields& f, const MediaD& m, const CpmlD& c, const ShotD& sh,
-                  const StoreD& st, const Grads& gr, int it);
-void launch_bwd_C(cudaStream_t s, const Geo& g, const Fields& f, const MediaD& m, const CpmlD& c, const ShotD& sh,
-                  const StoreD& st, const Grads& gr, int it, bool rev);
+// Tensor maps of the sweeps for one tile width: F1 stages vz, vx; F2 szz,
+// sxx, sxz; B vz, vx, szz_a, sxx_a, sxz_a; C vz_a, vx_a, szz, sxx, sxz.
+struct SweepMaps {
+  TileMaps f1, f2, b, c;
+};
+
+// Encodes the sweep tensor maps for tile width tx (host; needs the driver's
+// cuTensorMapEncodeTiled). Returns false with a message on failure.
+bool encode_sweep_maps(const Geo& g, const Fields& f, int tx, SweepMaps& out, const char** err);
+
+// ---- launchers (kernels.cu). tx selects the tile width; err is a device
+// word that a sweep sets when a bounded wait for its staged tiles gives up.
+void launch_fwd_stress(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
+                       const CpmlD& c, const ShotD& sh, const StoreD& st, int it, bool save, unsigned* err);
+void launch_fwd_velocity(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
+                         const CpmlD& c, unsigned* err);
+void launch_bwd_B(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
+                  const CpmlD& c, const ShotD& sh, const StoreD& st, const Grads& gr, int it, unsigned* err);
+void launch_bwd_C(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
+                  const CpmlD& c, const ShotD& sh, const StoreD& st, const Grads& gr, int it, bool rev,
+                  unsigned* err);
 
 // Model set-up: row-major double (lambda, mu in MPa) -> column-major float media.
 // cpmax_bits receives atomicMax of the P velocity's float bits.
-void launch_media_from_rowmajor(cudaStream_t s, int nz, int nx, const double* lam_mpa, const double* mu_mpa,
+void launch_media_from_rowmajor(cudaStream_t s, int nz, int nx, int ldz, const double* lam_mpa, const double* mu_mpa,
                                 const double* den, float* lam, float* mu, float* den_f, unsigned* cpmax_bits);
-void launch_media_derived(cudaStream_t s, int nz, int nx, const float* lam, const float* mu, const float* den,
-                          float* l2m, float* aveMu, float* bycA, float* bycB, float* hs, float* muw,
-                          unsigned* cpmax_bits);
+void launch_media_derived(cudaStream_t s, int nz, int nx, int ldz, const float* lam, const float* mu,
+                          const float* den, float* l2m, float* aveMu, float* bycA, float* bycB, float* hs,
+                          float* muw);
 
 // Residual: res = taper_r * (taper_o * obs - taper_o * syn) with sample 0
 // zeroed; syn is tapered in place. taper arrays are [nrec][nSteps] when
@@ -105,7 +136,7 @@ void launch_residual(cudaStream_t s, int nrec, int nSteps, const float* obs, flo
                      const float* taper_o, const float* taper_r, int per_trace, double* partials);
 void launch_sum_partials(cudaStream_t s, const double* partials, int n, double* acc);
 
-// Column-major float grid -> row-major double.
-void launch_to_rowmajor(cudaStream_t s, int nz, int nx, const float* src, double* dst, double scale);
+// Column-major float grid (stride ldz) -> row-major double.
+void launch_to_rowmajor(cudaStream_t s, int nz, int nx, int ldz, const float* src, double* dst, double scale);
 
 }  // namespace fwigb

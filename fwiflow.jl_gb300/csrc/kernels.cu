@@ -19,6 +19,10 @@
 // deterministic.
 #include "fwigb_kernels.h"
 
+#include <cudaTypedefs.h>
+
+#include <cstdint>
+
 namespace fwigb {
 namespace {
 
@@ -26,18 +30,76 @@ constexpr float C1 = 1.125f;          // 9/8  (el_stress.cu:42)
 constexpr float C2 = 1.0f / 24.0f;    // 1/24 (el_stress.cu:43)
 constexpr float kMega = 1.0e6f;       // MEGA (utilities.h:16)
 
-// Staggered 4th-order differences; Dm uses (i-2, i-1, i, i+1), Dp (i-1, i, i+1, i+2).
-__device__ __forceinline__ float dmz(const float* __restrict__ a, size_t i, float r) {
-  return (C1 * (a[i] - a[i - 1]) - C2 * (a[i + 1] - a[i - 2])) * r;
+// Bounded waits: a sweep that waits this many polls for its staged tiles
+// gives up, raises its error word and returns instead of hanging.
+constexpr unsigned kSpinLimit = 1u << 22;
+
+// ---- mbarrier / TMA (sm_90+ PTX; issued by one thread per block) ----
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
 }
-__device__ __forceinline__ float dpz(const float* __restrict__ a, size_t i, float r) {
-  return (C1 * (a[i + 1] - a[i]) - C2 * (a[i + 2] - a[i - 1])) * r;
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
-__device__ __forceinline__ float dmx(const float* __restrict__ a, size_t i, int nz, float r) {
-  return (C1 * (a[i] - a[i - nz]) - C2 * (a[i + nz] - a[i - 2 * nz])) * r;
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
-__device__ __forceinline__ float dpx(const float* __restrict__ a, size_t i, int nz, float r) {
-  return (C1 * (a[i + nz] - a[i]) - C2 * (a[i + 2 * nz] - a[i - nz])) * r;
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+  for (unsigned n = 0; n < kSpinLimit; ++n)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* tm, int c0, int c1, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Stages NA arrays of the tile at (z0, x0) into shared memory: one 2-D TMA
+// copy each of the box [z0-4, z0+36) x [x0-2, x0+TX+2) (zero filled outside
+// the grid). Returns false (after raising *err) if the bounded wait gives up.
+template <int NA, int TX>
+__device__ __forceinline__ bool stage_tiles(const TileMaps& mp, float* sm, uint64_t* bar, int z0, int x0,
+                                            unsigned* err) {
+  constexpr int N = kBoxZ * (TX + 4);
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(bar, NA * N * static_cast<unsigned>(sizeof(float)));
+#pragma unroll
+    for (int a = 0; a < NA; ++a) tma_load_2d(sm + a * N, &mp.t[a], z0 - 4, x0 - 2, bar);
+  }
+  if (!mbar_wait_bounded(bar, 0)) {
+    atomicOr(err, 1u);
+    mbar_wait_bounded(bar, 0);  // let copies still in flight land before the block exits
+    return false;
+  }
+  return true;
+}
+
+// Staggered 4th-order differences. Dm uses (i-2, i-1, i, i+1), Dp
+// (i-1, i, i+1, i+2); `s` is the stride of the direction (1 for z, the column
+// stride for x) and r the reciprocal spacing.
+__device__ __forceinline__ float dm(const float* __restrict__ a, long i, long s, float r) {
+  return (C1 * (a[i] - a[i - s]) - C2 * (a[i + s] - a[i - 2 * s])) * r;
+}
+__device__ __forceinline__ float dp(const float* __restrict__ a, long i, long s, float r) {
+  return (C1 * (a[i + s] - a[i]) - C2 * (a[i + 2 * s] - a[i - s])) * r;
 }
 
 // Index of cell (z, x) in the per-step boundary ring, or -1. Top and bottom
@@ -57,16 +119,45 @@ __device__ __forceinline__ bool in_box(int z, int x, int z0, int z1, int x0, int
   return z >= z0 && z <= z1 && x >= x0 && x <= x1;
 }
 
+// Receiver list of the 32 x 8 bin holding (z, x).
+__device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
+  const int b = (z / kBinZ) + (x / kBinX) * sh.nbin_z;
+  return make_int2(sh.blk_off[b], sh.blk_off[b + 1]);
+}
+
+// Thread layout of every sweep: lane = depth offset in the tile, warp w takes
+// the columns w, w+4, w+8, ... of the tile. `b` is the cell's index in a
+// staged box (column stride kBoxZ).
+#define SWEEP_PROLOGUE(NA)                                                     \
+  constexpr int N = kBoxZ * (TX + 4);                                          \
+  extern __shared__ __align__(128) float sm[];                                 \
+  __shared__ __align__(8) uint64_t bar;                                        \
+  const int z0 = blockIdx.x * kTileZ, x0 = blockIdx.y * TX;                    \
+  if (!stage_tiles<NA, TX>(mp, sm, &bar, z0, x0, err)) return;                 \
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;                   \
+  const int z = z0 + lane;                                                     \
+  const long ldz = g.ldz;                                                      \
+  (void)N;
+
+#define SWEEP_CELL_LOOP                                                        \
+  _Pragma("unroll 1") for (int lx = wid; lx < TX; lx += kSweepThreads / 32) {  \
+    const int x = x0 + lx;                                                     \
+    if (z >= g.nz || x >= g.nx) continue;                                      \
+    const long i = static_cast<long>(x) * ldz + z;                             \
+    const int b = (lx + 2) * kBoxZ + (lane + 4);
+
 // ---------------------------------------------------------------------------
 // F1: el_stress (el_stress.cu:50-88) + add_source (utilities.cu:521-541) +
 // recording (utilities.cu:557-567) + from_bnd of the 5 fields (Boundary.cu:55-76).
-__global__ void __launch_bounds__(kTileZ* kTileX)
-    k_fwd_stress(Geo g, Fields f, MediaD m, CpmlD c, ShotD sh, StoreD st, int it, int save) {
-  const int z = blockIdx.x * kTileZ + threadIdx.x;
-  const int x = blockIdx.y * kTileX + threadIdx.y;
-  if (z >= g.nz || x >= g.nx) return;
-  const int nz = g.nz;
-  const size_t i = static_cast<size_t>(x) * nz + z;
+// Staged: vz, vx.
+template <int TX>
+__global__ void __launch_bounds__(kSweepThreads)
+    k_fwd_stress(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c, ShotD sh, StoreD st,
+                 int it, int save, unsigned* err) {
+  SWEEP_PROLOGUE(2)
+  const float* s_vz = sm;
+  const float* s_vx = sm + N;
+  SWEEP_CELL_LOOP
   if (save) {
     const int k = ring_index(g, z, x);
     if (k >= 0) {
@@ -74,23 +165,19 @@ __global__ void __launch_bounds__(kTileZ* kTileX)
       p[0] = f.szz[i];
       p[g.ring_len] = f.sxz[i];
       p[2 * g.ring_len] = f.sxx[i];
-      p[3 * g.ring_len] = f.vz[i];
-      p[4 * g.ring_len] = f.vx[i];
+      p[3 * g.ring_len] = s_vz[b];
+      p[4 * g.ring_len] = s_vx[b];
     }
   }
   const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
   const bool src = (z == sh.src_z && x == sh.src_x);
   float szz = f.szz[i], sxx = f.sxx[i];
   if (dom) {
-    const float* __restrict__ vz = f.vz;
-    const float* __restrict__ vx = f.vx;
-    float dvz_dz = dmz(vz, i, g.rdz);
-    float dvx_dx = dmx(vx, i, nz, g.rdx);
-    float dvx_dz = dpz(vx, i, g.rdz);
-    float dvz_dx = dpx(vz, i, nz, g.rdx);
-    const bool zp = (z < g.nPml) || (z > g.zpml_hi);
-    const bool xp = (x < g.nPml) || (x > g.xpml_hi_s);
-    if (zp) {
+    float dvz_dz = dm(s_vz, b, 1, g.rdz);
+    float dvx_dx = dm(s_vx, b, kBoxZ, g.rdx);
+    float dvx_dz = dp(s_vx, b, 1, g.rdz);
+    float dvz_dx = dp(s_vz, b, kBoxZ, g.rdx);
+    if ((z < g.nPml) || (z > g.zpml_hi)) {
       float mm = c.b_z[z] * f.m_dvz_dz[i] + c.a_z[z] * dvz_dz;
       f.m_dvz_dz[i] = mm;
       dvz_dz = dvz_dz / c.K_z[z] + mm;
@@ -98,7 +185,7 @@ __global__ void __launch_bounds__(kTileZ* kTileX)
       f.m_dvx_dz[i] = mm;
       dvx_dz = dvx_dz / c.K_zh[z] + mm;
     }
-    if (xp) {
+    if ((x < g.nPml) || (x > g.xpml_hi_s)) {
       float mm = c.b_x[x] * f.m_dvx_dx[i] + c.a_x[x] * dvx_dx;
       f.m_dvx_dx[i] = mm;
       dvx_dx = dvx_dx / c.K_x[x] + mm;
@@ -120,31 +207,30 @@ __global__ void __launch_bounds__(kTileZ* kTileX)
     f.sxx[i] = sxx;
   }
   // The velocity sweep that follows does not change the stresses, so the
-  // sample of step it+1 can be taken here.
-  const int b = blockIdx.x + blockIdx.y * gridDim.x;
-  for (int k = sh.blk_off[b]; k < sh.blk_off[b + 1]; ++k) {
+  // sample of step it+1 is taken here.
+  const int2 rr = bin_range(sh, z, x);
+  for (int k = rr.x; k < rr.y; ++k) {
     const int r = sh.blk_rec[k];
     if (sh.rec_z[r] == z && sh.rec_x[r] == x) sh.data[static_cast<size_t>(r) * sh.nSteps + it + 1] = szz + 3.0f * sxx;
   }
+  }
 }
 
-// F2: el_velocity, isFor = true (el_velocity.cu:45-82).
-__global__ void __launch_bounds__(kTileZ* kTileX) k_fwd_velocity(Geo g, Fields f, MediaD m, CpmlD c) {
-  const int z = blockIdx.x * kTileZ + threadIdx.x;
-  const int x = blockIdx.y * kTileX + threadIdx.y;
-  if (!in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1)) return;
-  const int nz = g.nz;
-  const size_t i = static_cast<size_t>(x) * nz + z;
-  const float* __restrict__ szz = f.szz;
-  const float* __restrict__ sxx = f.sxx;
-  const float* __restrict__ sxz = f.sxz;
-  float dszz_dz = dpz(szz, i, g.rdz);
-  float dsxz_dx = dmx(sxz, i, nz, g.rdx);
-  float dsxz_dz = dmz(sxz, i, g.rdz);
-  float dsxx_dx = dpx(sxx, i, nz, g.rdx);
-  const bool zp = (z < g.nPml) || (z > g.zpml_hi);
-  const bool xp = (x < g.nPml) || (x > g.xpml_hi_v);
-  if (zp) {
+// F2: el_velocity, isFor = true (el_velocity.cu:45-82). Staged: szz, sxx, sxz.
+template <int TX>
+__global__ void __launch_bounds__(kSweepThreads)
+    k_fwd_velocity(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c, unsigned* err) {
+  SWEEP_PROLOGUE(3)
+  const float* s_szz = sm;
+  const float* s_sxx = sm + N;
+  const float* s_sxz = sm + 2 * N;
+  SWEEP_CELL_LOOP
+  if (!in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1)) continue;
+  float dszz_dz = dp(s_szz, b, 1, g.rdz);
+  float dsxz_dx = dm(s_sxz, b, kBoxZ, g.rdx);
+  float dsxz_dz = dm(s_sxz, b, 1, g.rdz);
+  float dsxx_dx = dp(s_sxx, b, kBoxZ, g.rdx);
+  if ((z < g.nPml) || (z > g.zpml_hi)) {
     float mm = c.b_zh[z] * f.m_dszz_dz[i] + c.a_zh[z] * dszz_dz;
     f.m_dszz_dz[i] = mm;
     dszz_dz = dszz_dz / c.K_zh[z] + mm;
@@ -152,7 +238,7 @@ __global__ void __launch_bounds__(kTileZ* kTileX) k_fwd_velocity(Geo g, Fields f
     f.m_dsxz_dz[i] = mm;
     dsxz_dz = dsxz_dz / c.K_z[z] + mm;
   }
-  if (xp) {
+  if ((x < g.nPml) || (x > g.xpml_hi_v)) {
     float mm = c.b_x[x] * f.m_dsxz_dx[i] + c.a_x[x] * dsxz_dx;
     f.m_dsxz_dx[i] = mm;
     dsxz_dx = dsxz_dx / c.K_x[x] + mm;
@@ -162,21 +248,24 @@ __global__ void __launch_bounds__(kTileZ* kTileX) k_fwd_velocity(Geo g, Fields f
   }
   f.vz[i] += (dszz_dz + dsxz_dx) * m.bycA[i] * g.dt;
   f.vx[i] += (dsxz_dz + dsxx_dx) * m.bycB[i] * g.dt;
+  }
 }
 
 // ---------------------------------------------------------------------------
-// B: add_source(-) + el_stress(isFor=false) + to_bnd(stress) + el_velocity_adj.
-__global__ void __launch_bounds__(kTileZ* kTileX)
-    k_bwd_B(Geo g, Fields f, MediaD m, CpmlD c, ShotD sh, StoreD st, Grads gr, int it) {
-  const int z = blockIdx.x * kTileZ + threadIdx.x;
-  const int x = blockIdx.y * kTileX + threadIdx.y;
-  if (z >= g.nz || x >= g.nx) return;
-  const int nz = g.nz;
-  const size_t i = static_cast<size_t>(x) * nz + z;
+// B: add_source(-) + el_stress(isFor=false) with the lambda / mu kernels +
+// to_bnd(stress) + el_velocity_adj. Staged: vz, vx, szz_a, sxx_a, sxz_a.
+template <int TX>
+__global__ void __launch_bounds__(kSweepThreads)
+    k_bwd_B(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c, ShotD sh, StoreD st, Grads gr,
+            int it, unsigned* err) {
+  SWEEP_PROLOGUE(5)
+  const float* s_vz = sm;
+  const float* s_vx = sm + N;
+  const float* s_szz_a = sm + 2 * N;
+  const float* s_sxx_a = sm + 3 * N;
+  const float* s_sxz_a = sm + 4 * N;
   const float dt = g.dt;
-  const float* __restrict__ vz = f.vz;
-  const float* __restrict__ vx = f.vx;
-  const float* __restrict__ sxz_a = f.sxz_a;
+  SWEEP_CELL_LOOP
   const bool interior = in_box(z, x, g.zi0, g.zi1, g.xi0, g.xi1);
   const bool src = (z == sh.src_z && x == sh.src_x);
   const int k = ring_index(g, z, x);
@@ -188,16 +277,16 @@ __global__ void __launch_bounds__(kTileZ* kTileX)
       sxx -= sh.src_sxx[it];
     }
     if (interior) {
-      const float dvz_dz = dmz(vz, i, g.rdz);
-      const float dvx_dx = dmx(vx, i, nz, g.rdx);
-      const float dvx_dz = dpz(vx, i, g.rdz);
-      const float dvz_dx = dpx(vz, i, nz, g.rdx);
+      const float dvz_dz = dm(s_vz, b, 1, g.rdz);
+      const float dvx_dx = dm(s_vx, b, kBoxZ, g.rdx);
+      const float dvx_dz = dp(s_vx, b, 1, g.rdz);
+      const float dvz_dx = dp(s_vz, b, kBoxZ, g.rdx);
       const float lam = m.lam[i], l2m = m.l2m[i];
       szz -= (l2m * dvz_dz + lam * dvx_dx) * dt;
       sxx -= (lam * dvz_dz + l2m * dvx_dx) * dt;
       e_own = dvx_dz + dvz_dx;
       sxz -= m.aveMu[i] * e_own * dt;
-      const float sa = f.szz_a[i], xa = f.sxx_a[i];
+      const float sa = s_szz_a[b], xa = s_sxx_a[b];
       gr.lam[i] += -(sa + xa) * (dvz_dz + dvx_dx) * dt * kMega;
       gmu_own = (-2.0f * sa * dvz_dz * dt - 2.0f * xa * dvx_dx * dt) * kMega;
     }
@@ -220,41 +309,42 @@ __global__ void __launch_bounds__(kTileZ* kTileX)
     const float* __restrict__ hs = m.hs;
     if (x <= g.xi1) {
       const float h = hs[i];
-      if (h != 0.0f) acc += w * (-sxz_a[i] * e_own * dt * h);
+      if (h != 0.0f) acc += w * (-s_sxz_a[b] * e_own * dt * h);
       if (z - 1 >= g.zi0) {
-        const size_t j = i - 1;
-        const float hj = hs[j];
-        if (hj != 0.0f) acc += w * (-sxz_a[j] * (dpz(vx, j, g.rdz) + dpx(vz, j, nz, g.rdx)) * dt * hj);
+        const float hj = hs[i - 1];
+        const int bj = b - 1;
+        if (hj != 0.0f)
+          acc += w * (-s_sxz_a[bj] * (dp(s_vx, bj, 1, g.rdz) + dp(s_vz, bj, kBoxZ, g.rdx)) * dt * hj);
       }
     }
     if (x - 1 >= g.xi0) {
-      const size_t j = i - nz;
-      const float hj = hs[j];
-      if (hj != 0.0f) acc += w * (-sxz_a[j] * (dpz(vx, j, g.rdz) + dpx(vz, j, nz, g.rdx)) * dt * hj);
+      const float hj = hs[i - ldz];
+      const int bj = b - kBoxZ;
+      if (hj != 0.0f) acc += w * (-s_sxz_a[bj] * (dp(s_vx, bj, 1, g.rdz) + dp(s_vz, bj, kBoxZ, g.rdx)) * dt * hj);
       if (z - 1 >= g.zi0 && x <= g.xi1) {
-        const size_t j2 = i - nz - 1;
-        const float h2 = hs[j2];
-        if (h2 != 0.0f) acc += w * (-sxz_a[j2] * (dpz(vx, j2, g.rdz) + dpx(vz, j2, nz, g.rdx)) * dt * h2);
+        const float h2 = hs[i - ldz - 1];
+        const int b2 = b - kBoxZ - 1;
+        if (h2 != 0.0f)
+          acc += w * (-s_sxz_a[b2] * (dp(s_vx, b2, 1, g.rdz) + dp(s_vz, b2, kBoxZ, g.rdx)) * dt * h2);
       }
     }
     gr.mu[i] = acc;
   }
-  // el_velocity_adj (el_velocity_adj.cu:161-206).
-  if (!in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1)) return;
-  const float* __restrict__ szz_a = f.szz_a;
-  const float* __restrict__ sxx_a = f.sxx_a;
+  // el_velocity_adj (el_velocity_adj.cu:161-206); the psi memory terms are
+  // read only where their CPML coefficient is non-zero.
+  if (!in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1)) continue;
   const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
   const bool zp = (z < g.nPml) || (z > g.zpml_hi);
   const bool xp = (x < g.nPml) || (x > g.xpml_hi_s);
   {
     const float Kx = c.K_x[x], Kzh = c.K_zh[z];
-    const float dszz_dx = -dpx(szz_a, i, nz, g.rdx);
-    const float dsxx_dx = -dpx(sxx_a, i, nz, g.rdx);
-    const float dsxz_dz = -dmz(sxz_a, i, g.rdz);
+    const float dszz_dx = -dp(s_szz_a, b, kBoxZ, g.rdx);
+    const float dsxx_dx = -dp(s_sxx_a, b, kBoxZ, g.rdx);
+    const float dsxz_dz = -dm(s_sxz_a, b, 1, g.rdz);
     float t = lam * dszz_dx / Kx * dt + l2m * dsxx_dx / Kx * dt + amu / Kzh * dsxz_dz * dt;
     const float ax = c.a_x[x], azh = c.a_zh[z];
-    if (ax != 0.0f) t += ax * (-dpx(f.m_dvx_dx, i, nz, g.rdx));
-    if (azh != 0.0f) t += azh * (-dmz(f.m_dvx_dz, i, g.rdz));
+    if (ax != 0.0f) t += ax * (-dp(f.m_dvx_dx, i, ldz, g.rdx));
+    if (azh != 0.0f) t += azh * (-dm(f.m_dvx_dz, i, 1, g.rdz));
     const float v = f.vx_a[i] + t;
     f.vx_a[i] = v;
     if (xp) f.m_dsxx_dx[i] = c.b_xh[x] * f.m_dsxx_dx[i] + m.bycB[i] * v * dt;
@@ -262,36 +352,42 @@ __global__ void __launch_bounds__(kTileZ* kTileX)
   }
   {
     const float Kz = c.K_z[z], Kxh = c.K_xh[x];
-    const float dszz_dz = -dpz(szz_a, i, g.rdz);
-    const float dsxx_dz = -dpz(sxx_a, i, g.rdz);
-    const float dsxz_dx = -dmx(sxz_a, i, nz, g.rdx);
+    const float dszz_dz = -dp(s_szz_a, b, 1, g.rdz);
+    const float dsxx_dz = -dp(s_sxx_a, b, 1, g.rdz);
+    const float dsxz_dx = -dm(s_sxz_a, b, kBoxZ, g.rdx);
     float t = l2m * dszz_dz / Kz * dt + lam * dsxx_dz / Kz * dt + amu / Kxh * dsxz_dx * dt;
     const float az = c.a_z[z], axh = c.a_xh[x];
-    if (az != 0.0f) t += az * (-dpz(f.m_dvz_dz, i, g.rdz));
-    if (axh != 0.0f) t += axh * (-dmx(f.m_dvz_dx, i, nz, g.rdx));
+    if (az != 0.0f) t += az * (-dp(f.m_dvz_dz, i, 1, g.rdz));
+    if (axh != 0.0f) t += axh * (-dm(f.m_dvz_dx, i, ldz, g.rdx));
     const float v = f.vz_a[i] + t;
     f.vz_a[i] = v;
     if (xp) f.m_dsxz_dx[i] = c.b_x[x] * f.m_dsxz_dx[i] + m.bycA[i] * v * dt;
     if (zp) f.m_dszz_dz[i] = c.b_zh[z] * f.m_dszz_dz[i] + m.bycA[i] * v * dt;
+  }
   }
 }
 
 // C: res_injection (utilities.cu:569-580) + el_stress_adj (el_stress_adj.cu:53-97)
 //    + source_grad (utilities.cu:582-593) + el_velocity(isFor=false) with the
 //    density kernel (el_velocity.cu:220-244) + to_bnd(velocity).
-__global__ void __launch_bounds__(kTileZ* kTileX)
-    k_bwd_C(Geo g, Fields f, MediaD m, CpmlD c, ShotD sh, StoreD st, Grads gr, int it, int rev) {
-  const int z = blockIdx.x * kTileZ + threadIdx.x;
-  const int x = blockIdx.y * kTileX + threadIdx.y;
-  if (z >= g.nz || x >= g.nx) return;
-  const int nz = g.nz;
-  const size_t i = static_cast<size_t>(x) * nz + z;
+//    Staged: vz_a, vx_a, szz, sxx, sxz.
+template <int TX>
+__global__ void __launch_bounds__(kSweepThreads)
+    k_bwd_C(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c, ShotD sh, StoreD st, Grads gr,
+            int it, int rev, unsigned* err) {
+  SWEEP_PROLOGUE(5)
+  const float* s_vz_a = sm;
+  const float* s_vx_a = sm + N;
+  const float* s_szz = sm + 2 * N;
+  const float* s_sxx = sm + 3 * N;
+  const float* s_sxz = sm + 4 * N;
   const float dt = g.dt;
+  SWEEP_CELL_LOOP
   const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
   float sa = f.szz_a[i], xa = f.sxx_a[i];
   bool injected = false;
-  const int b = blockIdx.x + blockIdx.y * gridDim.x;
-  for (int k = sh.blk_off[b]; k < sh.blk_off[b + 1]; ++k) {
+  const int2 rr = bin_range(sh, z, x);
+  for (int k = rr.x; k < rr.y; ++k) {
     const int r = sh.blk_rec[k];
     if (sh.rec_z[r] == z && sh.rec_x[r] == x) {
       const float rv = sh.res[static_cast<size_t>(r) * sh.nSteps + it];
@@ -301,18 +397,15 @@ __global__ void __launch_bounds__(kTileZ* kTileX)
     }
   }
   if (dom) {
-    const float* __restrict__ vz_a = f.vz_a;
-    const float* __restrict__ vx_a = f.vx_a;
     const float bA = m.bycA[i], bB = m.bycB[i], amu = m.aveMu[i];
-    // sxz
     float za = f.sxz_a[i];
     {
-      const float dvz_dx = -dpx(vz_a, i, nz, g.rdx);
-      const float dvx_dz = -dpz(vx_a, i, g.rdz);
+      const float dvz_dx = -dp(s_vz_a, b, kBoxZ, g.rdx);
+      const float dvx_dz = -dp(s_vx_a, b, 1, g.rdz);
       float t = dvz_dx / c.K_x[x] * bA * dt + dvx_dz / c.K_z[z] * bB * dt;
       const float ax = c.a_x[x], az = c.a_z[z];
-      if (ax != 0.0f) t += ax * (-dpx(f.m_dsxz_dx, i, nz, g.rdx));
-      if (az != 0.0f) t += az * (-dpz(f.m_dsxz_dz, i, g.rdz));
+      if (ax != 0.0f) t += ax * (-dp(f.m_dsxz_dx, i, ldz, g.rdx));
+      if (az != 0.0f) t += az * (-dp(f.m_dsxz_dz, i, 1, g.rdz));
       za += t;
       f.sxz_a[i] = za;
     }
@@ -321,13 +414,13 @@ __global__ void __launch_bounds__(kTileZ* kTileX)
     if (xb) f.m_dvz_dx[i] = c.b_xh[x] * f.m_dvz_dx[i] + za * amu * dt;
     if (zb) f.m_dvx_dz[i] = c.b_zh[z] * f.m_dvx_dz[i] + za * amu * dt;
     {
-      const float dvx_dx = -dmx(vx_a, i, nz, g.rdx);
-      const float dvz_dz = -dmz(vz_a, i, g.rdz);
+      const float dvx_dx = -dm(s_vx_a, b, kBoxZ, g.rdx);
+      const float dvz_dz = -dm(s_vz_a, b, 1, g.rdz);
       float tx = bB * dvx_dx / c.K_xh[x] * dt;
       float tz = bA * dvz_dz / c.K_zh[z] * dt;
       const float axh = c.a_xh[x], azh = c.a_zh[z];
-      if (axh != 0.0f) tx += axh * (-dmx(f.m_dsxx_dx, i, nz, g.rdx));
-      if (azh != 0.0f) tz += azh * (-dmz(f.m_dszz_dz, i, g.rdz));
+      if (axh != 0.0f) tx += axh * (-dm(f.m_dsxx_dx, i, ldz, g.rdx));
+      if (azh != 0.0f) tz += azh * (-dm(f.m_dszz_dz, i, 1, g.rdz));
       xa += tx;
       sa += tz;
     }
@@ -339,24 +432,18 @@ __global__ void __launch_bounds__(kTileZ* kTileX)
     f.szz_a[i] = sa;
     f.sxx_a[i] = xa;
   }
-  if (!rev) return;
+  if (!rev) continue;
   if (z == sh.src_z && x == sh.src_x) sh.gstf[it - 1] = -(sa + 3.0f * xa) * dt;
-
-  const float* __restrict__ szz = f.szz;
-  const float* __restrict__ sxx = f.sxx;
-  const float* __restrict__ sxz = f.sxz;
-  const float* __restrict__ vz_a = f.vz_a;
-  const float* __restrict__ vx_a = f.vx_a;
   const bool interior = in_box(z, x, g.zi0, g.zi1, g.xi0, g.xi1);
   float tA = 0.0f, tB = 0.0f;
   if (interior) {
-    const float ea = dpz(szz, i, g.rdz) + dmx(sxz, i, nz, g.rdx);  // dszz_dz + dsxz_dx
-    const float eb = dmz(sxz, i, g.rdz) + dpx(sxx, i, nz, g.rdx);  // dsxz_dz + dsxx_dx
+    const float ea = dp(s_szz, b, 1, g.rdz) + dm(s_sxz, b, kBoxZ, g.rdx);  // dszz_dz + dsxz_dx
+    const float eb = dm(s_sxz, b, 1, g.rdz) + dp(s_sxx, b, kBoxZ, g.rdx);  // dsxz_dz + dsxx_dx
     const float bA = m.bycA[i], bB = m.bycB[i];
     f.vz[i] -= ea * bA * dt;
     f.vx[i] -= eb * bB * dt;
-    tA = -vz_a[i] * ea * dt * (-bA * bA * 0.5f);
-    tB = -vx_a[i] * eb * dt * (-bB * bB * 0.5f);
+    tA = -s_vz_a[b] * ea * dt * (-bA * bA * 0.5f);
+    tB = -s_vx_a[b] * eb * dt * (-bB * bB * 0.5f);
   }
   const int k = ring_index(g, z, x);
   if (k >= 0) {
@@ -372,19 +459,20 @@ __global__ void __launch_bounds__(kTileZ* kTileX)
       acc += tA;
       acc += tB;
       if (z - 1 >= g.zi0) {
-        const size_t j = i - 1;
-        const float bA = m.bycA[j];
-        const float ea = dpz(szz, j, g.rdz) + dmx(sxz, j, nz, g.rdx);
-        acc += -vz_a[j] * ea * dt * (-bA * bA * 0.5f);
+        const int bj = b - 1;
+        const float bA = m.bycA[i - 1];
+        const float ea = dp(s_szz, bj, 1, g.rdz) + dm(s_sxz, bj, kBoxZ, g.rdx);
+        acc += -s_vz_a[bj] * ea * dt * (-bA * bA * 0.5f);
       }
     }
     if (x - 1 >= g.xi0) {
-      const size_t j = i - nz;
-      const float bB = m.bycB[j];
-      const float eb = dmz(sxz, j, g.rdz) + dpx(sxx, j, nz, g.rdx);
-      acc += -vx_a[j] * eb * dt * (-bB * bB * 0.5f);
+      const int bj = b - kBoxZ;
+      const float bB = m.bycB[i - ldz];
+      const float eb = dm(s_sxz, bj, 1, g.rdz) + dp(s_sxx, bj, kBoxZ, g.rdx);
+      acc += -s_vx_a[bj] * eb * dt * (-bB * bB * 0.5f);
     }
     gr.den[i] = acc;
+  }
   }
 }
 
@@ -394,9 +482,9 @@ constexpr int kT = 32;
 
 // Row-major double [nz][nx] (MPa) -> column-major float (Pa), through a
 // shared-memory tile so both sides are coalesced (libCUFD.cu:67-78).
-__global__ void k_media_from_rowmajor(int nz, int nx, const double* __restrict__ L, const double* __restrict__ M,
-                                      const double* __restrict__ D, float* lam, float* mu, float* den,
-                                      unsigned* cpmax_bits) {
+__global__ void k_media_from_rowmajor(int nz, int nx, int ldz, const double* __restrict__ L,
+                                      const double* __restrict__ M, const double* __restrict__ D, float* lam,
+                                      float* mu, float* den, unsigned* cpmax_bits) {
   __shared__ double tl[kT][kT + 1], tm[kT][kT + 1], td[kT][kT + 1];
   const int x0 = blockIdx.x * kT, z0 = blockIdx.y * kT;
   for (int r = threadIdx.y; r < kT; r += blockDim.y) {
@@ -413,7 +501,7 @@ __global__ void k_media_from_rowmajor(int nz, int nx, const double* __restrict__
   for (int r = threadIdx.y; r < kT; r += blockDim.y) {
     const int x = x0 + r, z = z0 + threadIdx.x;
     if (z < nz && x < nx) {
-      const size_t d = static_cast<size_t>(x) * nz + z;
+      const size_t d = static_cast<size_t>(x) * ldz + z;
       const float l = static_cast<float>(tl[threadIdx.x][r] * 1e6);
       const float u = static_cast<float>(tm[threadIdx.x][r] * 1e6);
       const float rho = static_cast<float>(td[threadIdx.x][r]);
@@ -430,26 +518,26 @@ __global__ void k_media_from_rowmajor(int nz, int nx, const double* __restrict__
 
 // aveMuInit / aveBycInit (utilities.cu:125-152) plus the terms of the fused
 // imaging sweeps.
-__global__ void k_media_derived(int nz, int nx, const float* __restrict__ lam, const float* __restrict__ mu,
-                                const float* __restrict__ den, float* l2m, float* aveMu, float* bycA, float* bycB,
-                                float* hs, float* muw) {
+__global__ void k_media_derived(int nz, int nx, int ldz, const float* __restrict__ lam,
+                                const float* __restrict__ mu, const float* __restrict__ den, float* l2m,
+                                float* aveMu, float* bycA, float* bycB, float* hs, float* muw) {
   const int z = blockIdx.x * blockDim.x + threadIdx.x;
   const int x = blockIdx.y * blockDim.y + threadIdx.y;
   if (z >= nz || x >= nx) return;
-  const size_t i = static_cast<size_t>(x) * nz + z;
+  const size_t i = static_cast<size_t>(x) * ldz + z;
   const float u = mu[i];
   l2m[i] = lam[i] + 2.0f * u;
   muw[i] = (u != 0.0f) ? static_cast<float>(1.0 / (static_cast<double>(u) * u)) : 0.0f;
   float am = 0.0f, ha = 0.0f, ba = 1.0f / 1000.0f, bb = 1.0f / 1000.0f;
   if (z >= 2 && z <= nz - 3 && x >= 2 && x <= nx - 3) {
-    const float a = u, b = mu[i + 1], c = mu[i + nz], d = mu[i + nz + 1];
+    const float a = u, b = mu[i + 1], c = mu[i + ldz], d = mu[i + ldz + 1];
     if (!(a == 0.0f || b == 0.0f || c == 0.0f || d == 0.0f)) {
       const double s = 1.0 / a + 1.0 / b + 1.0 / c + 1.0 / d;
       am = static_cast<float>(4.0 / s);
       ha = static_cast<float>(am / s * 1e6);
     }
     ba = static_cast<float>(2.0 / (den[i + 1] + den[i]));
-    bb = static_cast<float>(2.0 / (den[i + nz] + den[i]));
+    bb = static_cast<float>(2.0 / (den[i + ldz] + den[i]));
   }
   aveMu[i] = am;
   hs[i] = ha;
@@ -458,12 +546,12 @@ __global__ void k_media_derived(int nz, int nx, const float* __restrict__ lam, c
 }
 
 // Column-major float -> row-major double (libCUFD.cu:480-486).
-__global__ void k_to_rowmajor(int nz, int nx, const float* __restrict__ src, double* dst, double scale) {
+__global__ void k_to_rowmajor(int nz, int nx, int ldz, const float* __restrict__ src, double* dst, double scale) {
   __shared__ float t[kT][kT + 1];
   const int z0 = blockIdx.x * kT, x0 = blockIdx.y * kT;
   for (int r = threadIdx.y; r < kT; r += blockDim.y) {
     const int x = x0 + r, z = z0 + threadIdx.x;
-    if (z < nz && x < nx) t[r][threadIdx.x] = src[static_cast<size_t>(x) * nz + z];
+    if (z < nz && x < nx) t[r][threadIdx.x] = src[static_cast<size_t>(x) * ldz + z];
   }
   __syncthreads();
   for (int r = threadIdx.y; r < kT; r += blockDim.y) {
@@ -519,38 +607,118 @@ __global__ void k_sum_partials(const double* __restrict__ partials, int n, doubl
 }  // namespace
 
 // ---------------------------------------------------------------------------
-static dim3 sweep_grid(const Geo& g) { return dim3((g.nz + kTileZ - 1) / kTileZ, (g.nx + kTileX - 1) / kTileX); }
+namespace {
 
-void launch_fwd_stress(cudaStream_t s, const Geo& g, const Fields& f, const MediaD& m, const CpmlD& c,
-                       const ShotD& sh, const StoreD& st, int it, bool save) {
-  k_fwd_stress<<<sweep_grid(g), dim3(kTileZ, kTileX), 0, s>>>(g, f, m, c, sh, st, it, save ? 1 : 0);
+template <int TX>
+dim3 sweep_grid(const Geo& g) {
+  return dim3((g.nz + kTileZ - 1) / kTileZ, (g.nx + TX - 1) / TX);
+}
+template <int TX>
+constexpr size_t smem_bytes(int na) {
+  return static_cast<size_t>(na) * kBoxZ * (TX + 4) * sizeof(float);
 }
 
-void launch_fwd_velocity(cudaStream_t s, const Geo& g, const Fields& f, const MediaD& m, const CpmlD& c) {
-  k_fwd_velocity<<<sweep_grid(g), dim3(kTileZ, kTileX), 0, s>>>(g, f, m, c);
+}  // namespace
+
+#define FWIGB_DISPATCH_TX(tx, CALL) \
+  switch (tx) {                     \
+    case 8: {                       \
+      constexpr int TX = 8;         \
+      CALL;                         \
+      break;                        \
+    }                               \
+    case 16: {                      \
+      constexpr int TX = 16;        \
+      CALL;                         \
+      break;                        \
+    }                               \
+    default: {                      \
+      constexpr int TX = 32;        \
+      CALL;                         \
+      break;                        \
+    }                               \
+  }
+
+void launch_fwd_stress(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
+                       const CpmlD& c, const ShotD& sh, const StoreD& st, int it, bool save, unsigned* err) {
+  FWIGB_DISPATCH_TX(tx, (k_fwd_stress<TX><<<sweep_grid<TX>(g), kSweepThreads, smem_bytes<TX>(2), s>>>(
+                            mp, g, f, m, c, sh, st, it, save ? 1 : 0, err)))
 }
 
-void launch_bwd_B(cudaStream_t s, const Geo& g, const Fields& f, const MediaD& m, const CpmlD& c, const ShotD& sh,
-                  const StoreD& st, const Grads& gr, int it) {
-  k_bwd_B<<<sweep_grid(g), dim3(kTileZ, kTileX), 0, s>>>(g, f, m, c, sh, st, gr, it);
+void launch_fwd_velocity(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
+                         const CpmlD& c, unsigned* err) {
+  FWIGB_DISPATCH_TX(tx, (k_fwd_velocity<TX><<<sweep_grid<TX>(g), kSweepThreads, smem_bytes<TX>(3), s>>>(
+                            mp, g, f, m, c, err)))
 }
 
-void launch_bwd_C(cudaStream_t s, const Geo& g, const Fields& f, const MediaD& m, const CpmlD& c, const ShotD& sh,
-                  const StoreD& st, const Grads& gr, int it, bool rev) {
-  k_bwd_C<<<sweep_grid(g), dim3(kTileZ, kTileX), 0, s>>>(g, f, m, c, sh, st, gr, it, rev ? 1 : 0);
+void launch_bwd_B(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
+                  const CpmlD& c, const ShotD& sh, const StoreD& st, const Grads& gr, int it, unsigned* err) {
+  FWIGB_DISPATCH_TX(tx, (k_bwd_B<TX><<<sweep_grid<TX>(g), kSweepThreads, smem_bytes<TX>(5), s>>>(
+                            mp, g, f, m, c, sh, st, gr, it, err)))
 }
 
-void launch_media_from_rowmajor(cudaStream_t s, int nz, int nx, const double* lam_mpa, const double* mu_mpa,
+void launch_bwd_C(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
+                  const CpmlD& c, const ShotD& sh, const StoreD& st, const Grads& gr, int it, bool rev,
+                  unsigned* err) {
+  FWIGB_DISPATCH_TX(tx, (k_bwd_C<TX><<<sweep_grid<TX>(g), kSweepThreads, smem_bytes<TX>(5), s>>>(
+                            mp, g, f, m, c, sh, st, gr, it, rev ? 1 : 0, err)))
+}
+
+// Tensor maps: one per staged array, a 2-D view (z inner, x outer; row stride
+// ldz floats) with the box kBoxZ x (TX + 4). cuTensorMapEncodeTiled checks
+// the base (16-byte aligned: every array starts a multiple of ldz*nx floats
+// into a 256-byte aligned allocation) and the stride (ldz*4, a multiple of
+// 128); the x coordinate of every copy, z0 - 4 with z0 a multiple of 32, is a
+// multiple of 4 floats.
+bool encode_sweep_maps(const Geo& g, const Fields& f, int tx, SweepMaps& out, const char** err) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+      *err = "cuTensorMapEncodeTiled unavailable";
+      return false;
+    }
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  if (g.ldz % 32 != 0) {
+    *err = "column stride is not a multiple of 32 floats";
+    return false;
+  }
+  auto one = [&](CUtensorMap* m, float* base) {
+    if (reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(g.nz), static_cast<cuuint64_t>(g.nx)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(g.ldz) * sizeof(float)};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(kBoxZ), static_cast<cuuint32_t>(tx + 4)};
+    const cuuint32_t estr[2] = {1, 1};
+    return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  bool ok = true;
+  ok = ok && one(&out.f1.t[0], f.vz) && one(&out.f1.t[1], f.vx);
+  ok = ok && one(&out.f2.t[0], f.szz) && one(&out.f2.t[1], f.sxx) && one(&out.f2.t[2], f.sxz);
+  ok = ok && one(&out.b.t[0], f.vz) && one(&out.b.t[1], f.vx) && one(&out.b.t[2], f.szz_a) &&
+       one(&out.b.t[3], f.sxx_a) && one(&out.b.t[4], f.sxz_a);
+  ok = ok && one(&out.c.t[0], f.vz_a) && one(&out.c.t[1], f.vx_a) && one(&out.c.t[2], f.szz) &&
+       one(&out.c.t[3], f.sxx) && one(&out.c.t[4], f.sxz);
+  if (!ok) *err = "cuTensorMapEncodeTiled rejected a sweep tile";
+  return ok;
+}
+
+void launch_media_from_rowmajor(cudaStream_t s, int nz, int nx, int ldz, const double* lam_mpa, const double* mu_mpa,
                                 const double* den, float* lam, float* mu, float* den_f, unsigned* cpmax_bits) {
   dim3 grid((nx + kT - 1) / kT, (nz + kT - 1) / kT);
-  k_media_from_rowmajor<<<grid, dim3(kT, 8), 0, s>>>(nz, nx, lam_mpa, mu_mpa, den, lam, mu, den_f, cpmax_bits);
+  k_media_from_rowmajor<<<grid, dim3(kT, 8), 0, s>>>(nz, nx, ldz, lam_mpa, mu_mpa, den, lam, mu, den_f, cpmax_bits);
 }
 
-void launch_media_derived(cudaStream_t s, int nz, int nx, const float* lam, const float* mu, const float* den,
-                          float* l2m, float* aveMu, float* bycA, float* bycB, float* hs, float* muw,
-                          unsigned* /*cpmax_bits*/) {
+void launch_media_derived(cudaStream_t s, int nz, int nx, int ldz, const float* lam, const float* mu,
+                          const float* den, float* l2m, float* aveMu, float* bycA, float* bycB, float* hs,
+                          float* muw) {
   dim3 grid((nz + 31) / 32, (nx + 7) / 8);
-  k_media_derived<<<grid, dim3(32, 8), 0, s>>>(nz, nx, lam, mu, den, l2m, aveMu, bycA, bycB, hs, muw);
+  k_media_derived<<<grid, dim3(32, 8), 0, s>>>(nz, nx, ldz, lam, mu, den, l2m, aveMu, bycA, bycB, hs, muw);
 }
 
 int residual_blocks(int n) {
@@ -568,9 +736,9 @@ void launch_sum_partials(cudaStream_t s, const double* partials, int n, double* 
   k_sum_partials<<<1, 32, 0, s>>>(partials, n, acc);
 }
 
-void launch_to_rowmajor(cudaStream_t s, int nz, int nx, const float* src, double* dst, double scale) {
+void launch_to_rowmajor(cudaStream_t s, int nz, int nx, int ldz, const float* src, double* dst, double scale) {
   dim3 grid((nz + kT - 1) / kT, (nx + kT - 1) / kT);
-  k_to_rowmajor<<<grid, dim3(kT, 8), 0, s>>>(nz, nx, src, dst, scale);
+  k_to_rowmajor<<<grid, dim3(kT, 8), 0, s>>>(nz, nx, ldz, src, dst, scale);
 }
 
 }  // namespace fwigb

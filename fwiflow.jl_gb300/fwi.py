@@ -170,6 +170,17 @@ class FwiContext:
     def last_launch_count(self) -> int:
         return int(self._lib.fwigb_last_launch_count(self._h))
 
+    def tile_config(self):
+        """Tile widths of (forward stress, forward velocity, backward B, backward C)."""
+        t = np.zeros(4, dtype=np.int32)
+        _lib.check(self._lib.fwigb_tile_config(self._h, _lib.iptr(t)), self._h)
+        return [int(v) for v in t]
+
+    def set_tile_config(self, widths=None) -> None:
+        """Fix the four tile widths (8, 16 or 32); None re-enables the autotuner."""
+        t = None if widths is None else np.ascontiguousarray(widths, dtype=np.int32)
+        _lib.check(self._lib.fwigb_set_tile_config(self._h, _lib.iptr(t)), self._h)
+
     def set_kernel_timing(self, enable: bool) -> None:
         _lib.check(self._lib.fwigb_set_kernel_timing(self._h, int(enable)), self._h)
 

@@ -137,6 +137,13 @@ void *fwigb_stream(fwigb_ctx *ctx);
 /* Number of kernel launches the last fwigb_run issued (host-side count). */
 long long fwigb_last_launch_count(const fwigb_ctx *ctx);
 
+/* Tile widths (columns per thread block: 8, 16 or 32) of the four sweeps
+ * (forward stress, forward velocity, backward B, backward C). By default an
+ * autotuner times every width on the context's grid at the first run and keeps
+ * the fastest; fwigb_set_tile_config fixes them (NULL re-enables tuning). */
+int fwigb_tile_config(const fwigb_ctx *ctx, int *tile_x);
+int fwigb_set_tile_config(fwigb_ctx *ctx, const int *tile_x);
+
 /* Per-kernel timing of fwigb_run: when enabled, a CUDA event pair on the
  * context's stream brackets every sweep launch. Kinds: 0 forward stress,
  * 1 forward velocity, 2 backward sweep B, 3 backward sweep C. */
