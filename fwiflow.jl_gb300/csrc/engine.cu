@@ -330,8 +330,8 @@ struct fwigb_ctx {
   cudaStream_t stream = nullptr;
   size_t cells = 0;   // allocated cells per grid array (ldz * nx)
   size_t ncell = 0;   // logical cells (nz * nx), the size of host arrays
-  SweepMaps maps[3];  // tensor maps for tile widths 8, 16, 32
-  int tx[4] = {16, 16, 16, 16};  // tile width per sweep (F1, F2, B, C)
+  SweepMaps maps[3];  // tensor maps for tile widths 4, 8, 16
+  int tx[4] = {8, 8, 8, 8};  // tile width per sweep (F1, F2, B, C)
   bool tuned_fwd = false, tuned_bwd = false;
   bool autotune = true;
   // device buffers
@@ -371,7 +371,7 @@ thread_local std::string g_err;
     }                                                                                              \
   } while (0)
 
-int tx_slot(int tx) { return tx == 8 ? 0 : (tx == 16 ? 1 : 2); }
+int tx_slot(int tx) { return tx == 4 ? 0 : (tx == 8 ? 1 : 2); }
 
 Fields fields_of(fwigb_ctx* ctx) {
   float* b = ctx->fields.as<float>();
@@ -1091,8 +1091,8 @@ int fwigb_set_tile_config(fwigb_ctx* ctx, const int* tile_x) {
     return FWIGB_OK;
   }
   for (int k = 0; k < 4; ++k)
-    if (tile_x[k] != 8 && tile_x[k] != 16 && tile_x[k] != 32) {
-      ctx->err = "tile widths must be 8, 16 or 32";
+    if (tile_x[k] != 4 && tile_x[k] != 8 && tile_x[k] != 16) {
+      ctx->err = "tile widths must be 4, 8 or 16";
       return FWIGB_ERR_ARG;
     }
   for (int k = 0; k < 4; ++k) ctx->tx[k] = tile_x[k];

@@ -15,17 +15,16 @@
 
 namespace fwigb {
 
-// Sweep tiles: 32 depths (one per lane) x TX columns, TX in {8, 16, 32}
-// (chosen per sweep by the autotuner); 4 warps per block.
+// Sweep tiles: 32 depths x TX columns, one cell per thread (block 32 x TX),
+// TX in {4, 8, 16} chosen per sweep by the autotuner.
 constexpr int kTileZ = 32;
-constexpr int kSweepThreads = 128;
 // Receivers are binned on a fixed 32 x 8 grid, independent of the sweep tile.
 constexpr int kBinZ = 32;
 constexpr int kBinX = 8;
 // TMA box of one staged array: depths z0-4 .. z0+35 (start aligned to 16
 // bytes), columns x0-2 .. x0+TX+1.
 constexpr int kBoxZ = kTileZ + 8;
-constexpr int kTileXs[3] = {8, 16, 32};
+constexpr int kTileXs[3] = {4, 8, 16};
 
 // Tensor maps of the (up to 5) arrays a sweep stages into shared memory.
 struct alignas(64) TileMaps {

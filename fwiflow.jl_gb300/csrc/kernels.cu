@@ -67,38 +67,51 @@ __device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* tm, i
       : "memory");
 }
 
-// Stages NA arrays of the tile at (z0, x0) into shared memory: one 2-D TMA
-// copy each of the box [z0-4, z0+36) x [x0-2, x0+TX+2) (zero filled outside
-// the grid). Returns false (after raising *err) if the bounded wait gives up.
+// Starts staging NA arrays of the tile at (z0, x0) into shared memory: one
+// 2-D TMA copy each of the box [z0-4, z0+36) x [x0-2, x0+TX+2), zero filled
+// outside the grid. Thread (0,0) initialises the mbarrier and issues the
+// copies; the caller then loads its own-cell operands (which overlap with the
+// copies) and calls stage_wait.
 template <int NA, int TX>
-__device__ __forceinline__ bool stage_tiles(const TileMaps& mp, float* sm, uint64_t* bar, int z0, int x0,
-                                            unsigned* err) {
+__device__ __forceinline__ void stage_begin(const TileMaps& mp, float* sm, uint64_t* bar, int z0, int x0) {
   constexpr int N = kBoxZ * (TX + 4);
-  if (threadIdx.x == 0) {
+  const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
+  if (leader) {
     mbar_init(bar, 1);
     fence_mbar_init();
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (leader) {
     mbar_expect_tx(bar, NA * N * static_cast<unsigned>(sizeof(float)));
 #pragma unroll
     for (int a = 0; a < NA; ++a) tma_load_2d(sm + a * N, &mp.t[a], z0 - 4, x0 - 2, bar);
   }
-  if (!mbar_wait_bounded(bar, 0)) {
-    atomicOr(err, 1u);
-    mbar_wait_bounded(bar, 0);  // let copies still in flight land before the block exits
-    return false;
-  }
-  return true;
+}
+
+// Waits (bounded) for the staged tiles. On a timeout the error word is raised
+// and the thread waits once more so that copies still in flight land before
+// the block exits; the caller then returns without computing.
+__device__ __forceinline__ bool stage_wait(uint64_t* bar, unsigned* err) {
+  if (mbar_wait_bounded(bar, 0)) return true;
+  atomicOr(err, 1u);
+  mbar_wait_bounded(bar, 0);
+  return false;
 }
 
 // Staggered 4th-order differences. Dm uses (i-2, i-1, i, i+1), Dp
-// (i-1, i, i+1, i+2); `s` is the stride of the direction (1 for z, the column
-// stride for x) and r the reciprocal spacing.
-__device__ __forceinline__ float dm(const float* __restrict__ a, long i, long s, float r) {
+// (i-1, i, i+1, i+2); `s` is the stride of the direction and r the
+// reciprocal spacing. sdm / sdp read a staged tile (32-bit indices), gdm / gdp
+// global memory.
+__device__ __forceinline__ float sdm(const float* a, int i, int s, float r) {
   return (C1 * (a[i] - a[i - s]) - C2 * (a[i + s] - a[i - 2 * s])) * r;
 }
-__device__ __forceinline__ float dp(const float* __restrict__ a, long i, long s, float r) {
+__device__ __forceinline__ float sdp(const float* a, int i, int s, float r) {
+  return (C1 * (a[i + s] - a[i]) - C2 * (a[i + 2 * s] - a[i - s])) * r;
+}
+__device__ __forceinline__ float gdm(const float* __restrict__ a, size_t i, size_t s, float r) {
+  return (C1 * (a[i] - a[i - s]) - C2 * (a[i + s] - a[i - 2 * s])) * r;
+}
+__device__ __forceinline__ float gdp(const float* __restrict__ a, size_t i, size_t s, float r) {
   return (C1 * (a[i + s] - a[i]) - C2 * (a[i + 2 * s] - a[i - s])) * r;
 }
 
@@ -125,58 +138,59 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
   return make_int2(sh.blk_off[b], sh.blk_off[b + 1]);
 }
 
-// Thread layout of every sweep: lane = depth offset in the tile, warp w takes
-// the columns w, w+4, w+8, ... of the tile. `b` is the cell's index in a
-// staged box (column stride kBoxZ).
-#define SWEEP_PROLOGUE(NA)                                                     \
+// Thread layout of every sweep: block (32, TX), one cell per thread; lane
+// threadIdx.x is the depth offset, threadIdx.y the column offset in the tile.
+// `b` is the cell's index in a staged box (column stride kBoxZ).
+#define SWEEP_SETUP(NA)                                                        \
   constexpr int N = kBoxZ * (TX + 4);                                          \
   extern __shared__ __align__(128) float sm[];                                 \
   __shared__ __align__(8) uint64_t bar;                                        \
   const int z0 = blockIdx.x * kTileZ, x0 = blockIdx.y * TX;                    \
-  if (!stage_tiles<NA, TX>(mp, sm, &bar, z0, x0, err)) return;                 \
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;                   \
-  const int z = z0 + lane;                                                     \
-  const long ldz = g.ldz;                                                      \
-  (void)N;
+  stage_begin<NA, TX>(mp, sm, &bar, z0, x0);                                   \
+  const int z = z0 + threadIdx.x, x = x0 + threadIdx.y;                        \
+  if (z >= g.nz || x >= g.nx) return;                                          \
+  const size_t ldz = static_cast<size_t>(g.ldz);                               \
+  const size_t i = static_cast<size_t>(x) * ldz + z;                           \
+  const int b = (threadIdx.y + 2) * kBoxZ + threadIdx.x + 4;                   \
+  (void)N;                                                                     \
+  (void)b;
 
-#define SWEEP_CELL_LOOP                                                        \
-  _Pragma("unroll 1") for (int lx = wid; lx < TX; lx += kSweepThreads / 32) {  \
-    const int x = x0 + lx;                                                     \
-    if (z >= g.nz || x >= g.nx) continue;                                      \
-    const long i = static_cast<long>(x) * ldz + z;                             \
-    const int b = (lx + 2) * kBoxZ + (lane + 4);
+// Register budgets: forward sweeps 64 registers (32 warps per SM), backward
+// sweeps 80 (24 warps per SM).
+#define FWD_BOUNDS __launch_bounds__(32 * TX, 1024 / (32 * TX))
+#define BWD_BOUNDS __launch_bounds__(32 * TX, (768 / (32 * TX)) > 0 ? (768 / (32 * TX)) : 1)
 
 // ---------------------------------------------------------------------------
 // F1: el_stress (el_stress.cu:50-88) + add_source (utilities.cu:521-541) +
 // recording (utilities.cu:557-567) + from_bnd of the 5 fields (Boundary.cu:55-76).
 // Staged: vz, vx.
 template <int TX>
-__global__ void __launch_bounds__(kSweepThreads)
-    k_fwd_stress(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c, ShotD sh, StoreD st,
-                 int it, int save, unsigned* err) {
-  SWEEP_PROLOGUE(2)
+__global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c,
+                                        ShotD sh, StoreD st, int it, int save, unsigned* err) {
+  SWEEP_SETUP(2)
+  float szz = f.szz[i], sxx = f.sxx[i], sxz = f.sxz[i];
+  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
+  if (!stage_wait(&bar, err)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
-  SWEEP_CELL_LOOP
   if (save) {
     const int k = ring_index(g, z, x);
     if (k >= 0) {
       float* p = st.base + static_cast<size_t>(it) * 5 * g.ring_len + k;
-      p[0] = f.szz[i];
-      p[g.ring_len] = f.sxz[i];
-      p[2 * g.ring_len] = f.sxx[i];
+      p[0] = szz;
+      p[g.ring_len] = sxz;
+      p[2 * g.ring_len] = sxx;
       p[3 * g.ring_len] = s_vz[b];
       p[4 * g.ring_len] = s_vx[b];
     }
   }
   const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
   const bool src = (z == sh.src_z && x == sh.src_x);
-  float szz = f.szz[i], sxx = f.sxx[i];
   if (dom) {
-    float dvz_dz = dm(s_vz, b, 1, g.rdz);
-    float dvx_dx = dm(s_vx, b, kBoxZ, g.rdx);
-    float dvx_dz = dp(s_vx, b, 1, g.rdz);
-    float dvz_dx = dp(s_vz, b, kBoxZ, g.rdx);
+    float dvz_dz = sdm(s_vz, b, 1, g.rdz);
+    float dvx_dx = sdm(s_vx, b, kBoxZ, g.rdx);
+    float dvx_dz = sdp(s_vx, b, 1, g.rdz);
+    float dvz_dx = sdp(s_vz, b, kBoxZ, g.rdx);
     if ((z < g.nPml) || (z > g.zpml_hi)) {
       float mm = c.b_z[z] * f.m_dvz_dz[i] + c.a_z[z] * dvz_dz;
       f.m_dvz_dz[i] = mm;
@@ -193,10 +207,9 @@ __global__ void __launch_bounds__(kSweepThreads)
       f.m_dvz_dx[i] = mm;
       dvz_dx = dvz_dx / c.K_xh[x] + mm;
     }
-    const float lam = m.lam[i], l2m = m.l2m[i];
     szz += (l2m * dvz_dz + lam * dvx_dx) * g.dt;
     sxx += (lam * dvz_dz + l2m * dvx_dx) * g.dt;
-    f.sxz[i] = f.sxz[i] + m.aveMu[i] * (dvx_dz + dvz_dx) * g.dt;
+    f.sxz[i] = sxz + amu * (dvx_dz + dvz_dx) * g.dt;
   }
   if (src) {
     szz += sh.src_szz[it];
@@ -213,23 +226,29 @@ __global__ void __launch_bounds__(kSweepThreads)
     const int r = sh.blk_rec[k];
     if (sh.rec_z[r] == z && sh.rec_x[r] == x) sh.data[static_cast<size_t>(r) * sh.nSteps + it + 1] = szz + 3.0f * sxx;
   }
-  }
 }
 
 // F2: el_velocity, isFor = true (el_velocity.cu:45-82). Staged: szz, sxx, sxz.
 template <int TX>
-__global__ void __launch_bounds__(kSweepThreads)
-    k_fwd_velocity(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c, unsigned* err) {
-  SWEEP_PROLOGUE(3)
+__global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c,
+                                          unsigned* err) {
+  SWEEP_SETUP(3)
+  const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
+  float vz = 0.0f, vx = 0.0f, bA = 0.0f, bB = 0.0f;
+  if (dom) {
+    vz = f.vz[i];
+    vx = f.vx[i];
+    bA = m.bycA[i];
+    bB = m.bycB[i];
+  }
+  if (!stage_wait(&bar, err) || !dom) return;
   const float* s_szz = sm;
   const float* s_sxx = sm + N;
   const float* s_sxz = sm + 2 * N;
-  SWEEP_CELL_LOOP
-  if (!in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1)) continue;
-  float dszz_dz = dp(s_szz, b, 1, g.rdz);
-  float dsxz_dx = dm(s_sxz, b, kBoxZ, g.rdx);
-  float dsxz_dz = dm(s_sxz, b, 1, g.rdz);
-  float dsxx_dx = dp(s_sxx, b, kBoxZ, g.rdx);
+  float dszz_dz = sdp(s_szz, b, 1, g.rdz);
+  float dsxz_dx = sdm(s_sxz, b, kBoxZ, g.rdx);
+  float dsxz_dz = sdm(s_sxz, b, 1, g.rdz);
+  float dsxx_dx = sdp(s_sxx, b, kBoxZ, g.rdx);
   if ((z < g.nPml) || (z > g.zpml_hi)) {
     float mm = c.b_zh[z] * f.m_dszz_dz[i] + c.a_zh[z] * dszz_dz;
     f.m_dszz_dz[i] = mm;
@@ -246,48 +265,48 @@ __global__ void __launch_bounds__(kSweepThreads)
     f.m_dsxx_dx[i] = mm;
     dsxx_dx = dsxx_dx / c.K_xh[x] + mm;
   }
-  f.vz[i] += (dszz_dz + dsxz_dx) * m.bycA[i] * g.dt;
-  f.vx[i] += (dsxz_dz + dsxx_dx) * m.bycB[i] * g.dt;
-  }
+  f.vz[i] = vz + (dszz_dz + dsxz_dx) * bA * g.dt;
+  f.vx[i] = vx + (dsxz_dz + dsxx_dx) * bB * g.dt;
 }
 
 // ---------------------------------------------------------------------------
 // B: add_source(-) + el_stress(isFor=false) with the lambda / mu kernels +
 // to_bnd(stress) + el_velocity_adj. Staged: vz, vx, szz_a, sxx_a, sxz_a.
 template <int TX>
-__global__ void __launch_bounds__(kSweepThreads)
-    k_bwd_B(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c, ShotD sh, StoreD st, Grads gr,
-            int it, unsigned* err) {
-  SWEEP_PROLOGUE(5)
+__global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c, ShotD sh,
+                                   StoreD st, Grads gr, int it, unsigned* err) {
+  SWEEP_SETUP(5)
+  const float dt = g.dt;
+  float szz = f.szz[i], sxx = f.sxx[i], sxz = f.sxz[i];
+  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
+  const float gl = gr.lam[i], gm = gr.mu[i], w = m.muw[i], h = m.hs[i];
+  const float va_z = f.vz_a[i], va_x = f.vx_a[i], bA = m.bycA[i], bB = m.bycB[i];
+  if (!stage_wait(&bar, err)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
   const float* s_szz_a = sm + 2 * N;
   const float* s_sxx_a = sm + 3 * N;
   const float* s_sxz_a = sm + 4 * N;
-  const float dt = g.dt;
-  SWEEP_CELL_LOOP
   const bool interior = in_box(z, x, g.zi0, g.zi1, g.xi0, g.xi1);
   const bool src = (z == sh.src_z && x == sh.src_x);
   const int k = ring_index(g, z, x);
   float e_own = 0.0f, gmu_own = 0.0f;
   if (interior || src || k >= 0) {
-    float szz = f.szz[i], sxx = f.sxx[i], sxz = f.sxz[i];
     if (src) {
       szz -= sh.src_szz[it];
       sxx -= sh.src_sxx[it];
     }
     if (interior) {
-      const float dvz_dz = dm(s_vz, b, 1, g.rdz);
-      const float dvx_dx = dm(s_vx, b, kBoxZ, g.rdx);
-      const float dvx_dz = dp(s_vx, b, 1, g.rdz);
-      const float dvz_dx = dp(s_vz, b, kBoxZ, g.rdx);
-      const float lam = m.lam[i], l2m = m.l2m[i];
+      const float dvz_dz = sdm(s_vz, b, 1, g.rdz);
+      const float dvx_dx = sdm(s_vx, b, kBoxZ, g.rdx);
+      const float dvx_dz = sdp(s_vx, b, 1, g.rdz);
+      const float dvz_dx = sdp(s_vz, b, kBoxZ, g.rdx);
       szz -= (l2m * dvz_dz + lam * dvx_dx) * dt;
       sxx -= (lam * dvz_dz + l2m * dvx_dx) * dt;
       e_own = dvx_dz + dvz_dx;
-      sxz -= m.aveMu[i] * e_own * dt;
+      sxz -= amu * e_own * dt;
       const float sa = s_szz_a[b], xa = s_sxx_a[b];
-      gr.lam[i] += -(sa + xa) * (dvz_dz + dvx_dx) * dt * kMega;
+      gr.lam[i] = gl + -(sa + xa) * (dvz_dz + dvx_dx) * dt * kMega;
       gmu_own = (-2.0f * sa * dvz_dz * dt - 2.0f * xa * dvx_dx * dt) * kMega;
     }
     if (k >= 0) {
@@ -304,66 +323,62 @@ __global__ void __launch_bounds__(kSweepThreads)
   // whose top-left corner is (z,x), (z-1,x), (z,x-1), (z-1,x-1), with the
   // guards of el_stress.cu:118-123 (the x guard of :120 is always true).
   if (in_box(z, x, g.zi0, g.zi1, g.xi0, g.xi1 + 1)) {
-    float acc = gr.mu[i] + gmu_own;
-    const float w = m.muw[i];
+    float acc = gm + gmu_own;
     const float* __restrict__ hs = m.hs;
     if (x <= g.xi1) {
-      const float h = hs[i];
       if (h != 0.0f) acc += w * (-s_sxz_a[b] * e_own * dt * h);
       if (z - 1 >= g.zi0) {
         const float hj = hs[i - 1];
         const int bj = b - 1;
         if (hj != 0.0f)
-          acc += w * (-s_sxz_a[bj] * (dp(s_vx, bj, 1, g.rdz) + dp(s_vz, bj, kBoxZ, g.rdx)) * dt * hj);
+          acc += w * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, kBoxZ, g.rdx)) * dt * hj);
       }
     }
     if (x - 1 >= g.xi0) {
       const float hj = hs[i - ldz];
       const int bj = b - kBoxZ;
-      if (hj != 0.0f) acc += w * (-s_sxz_a[bj] * (dp(s_vx, bj, 1, g.rdz) + dp(s_vz, bj, kBoxZ, g.rdx)) * dt * hj);
+      if (hj != 0.0f) acc += w * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, kBoxZ, g.rdx)) * dt * hj);
       if (z - 1 >= g.zi0 && x <= g.xi1) {
         const float h2 = hs[i - ldz - 1];
         const int b2 = b - kBoxZ - 1;
         if (h2 != 0.0f)
-          acc += w * (-s_sxz_a[b2] * (dp(s_vx, b2, 1, g.rdz) + dp(s_vz, b2, kBoxZ, g.rdx)) * dt * h2);
+          acc += w * (-s_sxz_a[b2] * (sdp(s_vx, b2, 1, g.rdz) + sdp(s_vz, b2, kBoxZ, g.rdx)) * dt * h2);
       }
     }
     gr.mu[i] = acc;
   }
   // el_velocity_adj (el_velocity_adj.cu:161-206); the psi memory terms are
   // read only where their CPML coefficient is non-zero.
-  if (!in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1)) continue;
-  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
+  if (!in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1)) return;
   const bool zp = (z < g.nPml) || (z > g.zpml_hi);
   const bool xp = (x < g.nPml) || (x > g.xpml_hi_s);
   {
     const float Kx = c.K_x[x], Kzh = c.K_zh[z];
-    const float dszz_dx = -dp(s_szz_a, b, kBoxZ, g.rdx);
-    const float dsxx_dx = -dp(s_sxx_a, b, kBoxZ, g.rdx);
-    const float dsxz_dz = -dm(s_sxz_a, b, 1, g.rdz);
+    const float dszz_dx = -sdp(s_szz_a, b, kBoxZ, g.rdx);
+    const float dsxx_dx = -sdp(s_sxx_a, b, kBoxZ, g.rdx);
+    const float dsxz_dz = -sdm(s_sxz_a, b, 1, g.rdz);
     float t = lam * dszz_dx / Kx * dt + l2m * dsxx_dx / Kx * dt + amu / Kzh * dsxz_dz * dt;
     const float ax = c.a_x[x], azh = c.a_zh[z];
-    if (ax != 0.0f) t += ax * (-dp(f.m_dvx_dx, i, ldz, g.rdx));
-    if (azh != 0.0f) t += azh * (-dm(f.m_dvx_dz, i, 1, g.rdz));
-    const float v = f.vx_a[i] + t;
+    if (ax != 0.0f) t += ax * (-gdp(f.m_dvx_dx, i, ldz, g.rdx));
+    if (azh != 0.0f) t += azh * (-gdm(f.m_dvx_dz, i, 1, g.rdz));
+    const float v = va_x + t;
     f.vx_a[i] = v;
-    if (xp) f.m_dsxx_dx[i] = c.b_xh[x] * f.m_dsxx_dx[i] + m.bycB[i] * v * dt;
-    if (zp) f.m_dsxz_dz[i] = c.b_z[z] * f.m_dsxz_dz[i] + m.bycB[i] * v * dt;
+    if (xp) f.m_dsxx_dx[i] = c.b_xh[x] * f.m_dsxx_dx[i] + bB * v * dt;
+    if (zp) f.m_dsxz_dz[i] = c.b_z[z] * f.m_dsxz_dz[i] + bB * v * dt;
   }
   {
     const float Kz = c.K_z[z], Kxh = c.K_xh[x];
-    const float dszz_dz = -dp(s_szz_a, b, 1, g.rdz);
-    const float dsxx_dz = -dp(s_sxx_a, b, 1, g.rdz);
-    const float dsxz_dx = -dm(s_sxz_a, b, kBoxZ, g.rdx);
+    const float dszz_dz = -sdp(s_szz_a, b, 1, g.rdz);
+    const float dsxx_dz = -sdp(s_sxx_a, b, 1, g.rdz);
+    const float dsxz_dx = -sdm(s_sxz_a, b, kBoxZ, g.rdx);
     float t = l2m * dszz_dz / Kz * dt + lam * dsxx_dz / Kz * dt + amu / Kxh * dsxz_dx * dt;
     const float az = c.a_z[z], axh = c.a_xh[x];
-    if (az != 0.0f) t += az * (-dp(f.m_dvz_dz, i, 1, g.rdz));
-    if (axh != 0.0f) t += axh * (-dm(f.m_dvz_dx, i, ldz, g.rdx));
-    const float v = f.vz_a[i] + t;
+    if (az != 0.0f) t += az * (-gdp(f.m_dvz_dz, i, 1, g.rdz));
+    if (axh != 0.0f) t += axh * (-gdm(f.m_dvz_dx, i, ldz, g.rdx));
+    const float v = va_z + t;
     f.vz_a[i] = v;
-    if (xp) f.m_dsxz_dx[i] = c.b_x[x] * f.m_dsxz_dx[i] + m.bycA[i] * v * dt;
-    if (zp) f.m_dszz_dz[i] = c.b_zh[z] * f.m_dszz_dz[i] + m.bycA[i] * v * dt;
-  }
+    if (xp) f.m_dsxz_dx[i] = c.b_x[x] * f.m_dsxz_dx[i] + bA * v * dt;
+    if (zp) f.m_dszz_dz[i] = c.b_zh[z] * f.m_dszz_dz[i] + bA * v * dt;
   }
 }
 
@@ -372,19 +387,25 @@ __global__ void __launch_bounds__(kSweepThreads)
 //    density kernel (el_velocity.cu:220-244) + to_bnd(velocity).
 //    Staged: vz_a, vx_a, szz, sxx, sxz.
 template <int TX>
-__global__ void __launch_bounds__(kSweepThreads)
-    k_bwd_C(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c, ShotD sh, StoreD st, Grads gr,
-            int it, int rev, unsigned* err) {
-  SWEEP_PROLOGUE(5)
+__global__ void BWD_BOUNDS k_bwd_C(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c, ShotD sh,
+                                   StoreD st, Grads gr, int it, int rev, unsigned* err) {
+  SWEEP_SETUP(5)
+  const float dt = g.dt;
+  float sa = f.szz_a[i], xa = f.sxx_a[i], za = f.sxz_a[i];
+  const float bA = m.bycA[i], bB = m.bycB[i], amu = m.aveMu[i], lam = m.lam[i], l2m = m.l2m[i];
+  float vz = 0.0f, vx = 0.0f, gd = 0.0f;
+  if (rev) {
+    vz = f.vz[i];
+    vx = f.vx[i];
+    gd = gr.den[i];
+  }
+  if (!stage_wait(&bar, err)) return;
   const float* s_vz_a = sm;
   const float* s_vx_a = sm + N;
   const float* s_szz = sm + 2 * N;
   const float* s_sxx = sm + 3 * N;
   const float* s_sxz = sm + 4 * N;
-  const float dt = g.dt;
-  SWEEP_CELL_LOOP
   const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
-  float sa = f.szz_a[i], xa = f.sxx_a[i];
   bool injected = false;
   const int2 rr = bin_range(sh, z, x);
   for (int k = rr.x; k < rr.y; ++k) {
@@ -397,15 +418,13 @@ __global__ void __launch_bounds__(kSweepThreads)
     }
   }
   if (dom) {
-    const float bA = m.bycA[i], bB = m.bycB[i], amu = m.aveMu[i];
-    float za = f.sxz_a[i];
     {
-      const float dvz_dx = -dp(s_vz_a, b, kBoxZ, g.rdx);
-      const float dvx_dz = -dp(s_vx_a, b, 1, g.rdz);
+      const float dvz_dx = -sdp(s_vz_a, b, kBoxZ, g.rdx);
+      const float dvx_dz = -sdp(s_vx_a, b, 1, g.rdz);
       float t = dvz_dx / c.K_x[x] * bA * dt + dvx_dz / c.K_z[z] * bB * dt;
       const float ax = c.a_x[x], az = c.a_z[z];
-      if (ax != 0.0f) t += ax * (-dp(f.m_dsxz_dx, i, ldz, g.rdx));
-      if (az != 0.0f) t += az * (-dp(f.m_dsxz_dz, i, 1, g.rdz));
+      if (ax != 0.0f) t += ax * (-gdp(f.m_dsxz_dx, i, ldz, g.rdx));
+      if (az != 0.0f) t += az * (-gdp(f.m_dsxz_dz, i, 1, g.rdz));
       za += t;
       f.sxz_a[i] = za;
     }
@@ -414,17 +433,16 @@ __global__ void __launch_bounds__(kSweepThreads)
     if (xb) f.m_dvz_dx[i] = c.b_xh[x] * f.m_dvz_dx[i] + za * amu * dt;
     if (zb) f.m_dvx_dz[i] = c.b_zh[z] * f.m_dvx_dz[i] + za * amu * dt;
     {
-      const float dvx_dx = -dm(s_vx_a, b, kBoxZ, g.rdx);
-      const float dvz_dz = -dm(s_vz_a, b, 1, g.rdz);
+      const float dvx_dx = -sdm(s_vx_a, b, kBoxZ, g.rdx);
+      const float dvz_dz = -sdm(s_vz_a, b, 1, g.rdz);
       float tx = bB * dvx_dx / c.K_xh[x] * dt;
       float tz = bA * dvz_dz / c.K_zh[z] * dt;
       const float axh = c.a_xh[x], azh = c.a_zh[z];
-      if (axh != 0.0f) tx += axh * (-dm(f.m_dsxx_dx, i, ldz, g.rdx));
-      if (azh != 0.0f) tz += azh * (-dm(f.m_dszz_dz, i, 1, g.rdz));
+      if (axh != 0.0f) tx += axh * (-gdm(f.m_dsxx_dx, i, ldz, g.rdx));
+      if (azh != 0.0f) tz += azh * (-gdm(f.m_dszz_dz, i, 1, g.rdz));
       xa += tx;
       sa += tz;
     }
-    const float lam = m.lam[i], l2m = m.l2m[i];
     if (xb) f.m_dvx_dx[i] = c.b_x[x] * f.m_dvx_dx[i] + lam * sa * dt + l2m * xa * dt;
     if (zb) f.m_dvz_dz[i] = c.b_z[z] * f.m_dvz_dz[i] + l2m * sa * dt + lam * xa * dt;
   }
@@ -432,47 +450,49 @@ __global__ void __launch_bounds__(kSweepThreads)
     f.szz_a[i] = sa;
     f.sxx_a[i] = xa;
   }
-  if (!rev) continue;
+  if (!rev) return;
   if (z == sh.src_z && x == sh.src_x) sh.gstf[it - 1] = -(sa + 3.0f * xa) * dt;
   const bool interior = in_box(z, x, g.zi0, g.zi1, g.xi0, g.xi1);
   float tA = 0.0f, tB = 0.0f;
+  const int k = ring_index(g, z, x);
   if (interior) {
-    const float ea = dp(s_szz, b, 1, g.rdz) + dm(s_sxz, b, kBoxZ, g.rdx);  // dszz_dz + dsxz_dx
-    const float eb = dm(s_sxz, b, 1, g.rdz) + dp(s_sxx, b, kBoxZ, g.rdx);  // dsxz_dz + dsxx_dx
-    const float bA = m.bycA[i], bB = m.bycB[i];
-    f.vz[i] -= ea * bA * dt;
-    f.vx[i] -= eb * bB * dt;
+    const float ea = sdp(s_szz, b, 1, g.rdz) + sdm(s_sxz, b, kBoxZ, g.rdx);  // dszz_dz + dsxz_dx
+    const float eb = sdm(s_sxz, b, 1, g.rdz) + sdp(s_sxx, b, kBoxZ, g.rdx);  // dsxz_dz + dsxx_dx
+    vz -= ea * bA * dt;
+    vx -= eb * bB * dt;
     tA = -s_vz_a[b] * ea * dt * (-bA * bA * 0.5f);
     tB = -s_vx_a[b] * eb * dt * (-bB * bB * 0.5f);
   }
-  const int k = ring_index(g, z, x);
   if (k >= 0) {
     const float* p = st.base + static_cast<size_t>(it - 1) * 5 * g.ring_len + k;
-    f.vz[i] = p[3 * g.ring_len];
-    f.vx[i] = p[4 * g.ring_len];
+    vz = p[3 * g.ring_len];
+    vx = p[4 * g.ring_len];
+  }
+  if (interior || k >= 0) {
+    f.vz[i] = vz;
+    f.vx[i] = vx;
   }
   // rho kernel gather: (z,x) receives A and B of itself, A of (z-1,x) and B of
   // (z,x-1) (el_velocity.cu:238-243; the x guard of :242 is always true).
   if (in_box(z, x, g.zi0, g.zi1, g.xi0, g.xi1 + 1)) {
-    float acc = gr.den[i];
+    float acc = gd;
     if (x <= g.xi1) {
       acc += tA;
       acc += tB;
       if (z - 1 >= g.zi0) {
         const int bj = b - 1;
-        const float bA = m.bycA[i - 1];
-        const float ea = dp(s_szz, bj, 1, g.rdz) + dm(s_sxz, bj, kBoxZ, g.rdx);
-        acc += -s_vz_a[bj] * ea * dt * (-bA * bA * 0.5f);
+        const float bAj = m.bycA[i - 1];
+        const float ea = sdp(s_szz, bj, 1, g.rdz) + sdm(s_sxz, bj, kBoxZ, g.rdx);
+        acc += -s_vz_a[bj] * ea * dt * (-bAj * bAj * 0.5f);
       }
     }
     if (x - 1 >= g.xi0) {
       const int bj = b - kBoxZ;
-      const float bB = m.bycB[i - ldz];
-      const float eb = dm(s_sxz, bj, 1, g.rdz) + dp(s_sxx, bj, kBoxZ, g.rdx);
-      acc += -s_vx_a[bj] * eb * dt * (-bB * bB * 0.5f);
+      const float bBj = m.bycB[i - ldz];
+      const float eb = sdm(s_sxz, bj, 1, g.rdz) + sdp(s_sxx, bj, kBoxZ, g.rdx);
+      acc += -s_vx_a[bj] * eb * dt * (-bBj * bBj * 0.5f);
     }
     gr.den[i] = acc;
-  }
   }
 }
 
@@ -622,18 +642,18 @@ constexpr size_t smem_bytes(int na) {
 
 #define FWIGB_DISPATCH_TX(tx, CALL) \
   switch (tx) {                     \
+    case 4: {                       \
+      constexpr int TX = 4;         \
+      CALL;                         \
+      break;                        \
+    }                               \
     case 8: {                       \
       constexpr int TX = 8;         \
       CALL;                         \
       break;                        \
     }                               \
-    case 16: {                      \
-      constexpr int TX = 16;        \
-      CALL;                         \
-      break;                        \
-    }                               \
     default: {                      \
-      constexpr int TX = 32;        \
+      constexpr int TX = 16;        \
       CALL;                         \
       break;                        \
     }                               \
@@ -641,26 +661,26 @@ constexpr size_t smem_bytes(int na) {
 
 void launch_fwd_stress(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
                        const CpmlD& c, const ShotD& sh, const StoreD& st, int it, bool save, unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, (k_fwd_stress<TX><<<sweep_grid<TX>(g), kSweepThreads, smem_bytes<TX>(2), s>>>(
+  FWIGB_DISPATCH_TX(tx, (k_fwd_stress<TX><<<sweep_grid<TX>(g), dim3(32, TX), smem_bytes<TX>(2), s>>>(
                             mp, g, f, m, c, sh, st, it, save ? 1 : 0, err)))
 }
 
 void launch_fwd_velocity(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
                          const CpmlD& c, unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, (k_fwd_velocity<TX><<<sweep_grid<TX>(g), kSweepThreads, smem_bytes<TX>(3), s>>>(
+  FWIGB_DISPATCH_TX(tx, (k_fwd_velocity<TX><<<sweep_grid<TX>(g), dim3(32, TX), smem_bytes<TX>(3), s>>>(
                             mp, g, f, m, c, err)))
 }
 
 void launch_bwd_B(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
                   const CpmlD& c, const ShotD& sh, const StoreD& st, const Grads& gr, int it, unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, (k_bwd_B<TX><<<sweep_grid<TX>(g), kSweepThreads, smem_bytes<TX>(5), s>>>(
+  FWIGB_DISPATCH_TX(tx, (k_bwd_B<TX><<<sweep_grid<TX>(g), dim3(32, TX), smem_bytes<TX>(5), s>>>(
                             mp, g, f, m, c, sh, st, gr, it, err)))
 }
 
 void launch_bwd_C(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
                   const CpmlD& c, const ShotD& sh, const StoreD& st, const Grads& gr, int it, bool rev,
                   unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, (k_bwd_C<TX><<<sweep_grid<TX>(g), kSweepThreads, smem_bytes<TX>(5), s>>>(
+  FWIGB_DISPATCH_TX(tx, (k_bwd_C<TX><<<sweep_grid<TX>(g), dim3(32, TX), smem_bytes<TX>(5), s>>>(
                             mp, g, f, m, c, sh, st, gr, it, rev ? 1 : 0, err)))
 }
 

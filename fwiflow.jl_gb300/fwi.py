@@ -177,7 +177,7 @@ class FwiContext:
         return [int(v) for v in t]
 
     def set_tile_config(self, widths=None) -> None:
-        """Fix the four tile widths (8, 16 or 32); None re-enables the autotuner."""
+        """Fix the four tile widths (4, 8 or 16); None re-enables the autotuner."""
         t = None if widths is None else np.ascontiguousarray(widths, dtype=np.int32)
         _lib.check(self._lib.fwigb_set_tile_config(self._h, _lib.iptr(t)), self._h)
 

@@ -137,7 +137,7 @@ void *fwigb_stream(fwigb_ctx *ctx);
 /* Number of kernel launches the last fwigb_run issued (host-side count). */
 long long fwigb_last_launch_count(const fwigb_ctx *ctx);
 
-/* Tile widths (columns per thread block: 8, 16 or 32) of the four sweeps
+/* Tile widths (columns per thread block: 4, 8 or 16) of the four sweeps
  * (forward stress, forward velocity, backward B, backward C). By default an
  * autotuner times every width on the context's grid at the first run and keeps
  * the fastest; fwigb_set_tile_config fixes them (NULL re-enables tuning). */
