@@ -3,7 +3,8 @@ throughput (Gpts/s = grid cells x time steps x shots per second of one
 misfit + gradient evaluation) against the HBM roofline.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload dipping_grf|small_layered] [--no-cpu-baseline]
+                    [--workload dipping_grf|small_layered|batched_uneven] [--shots S]
+                    [--compare-single] [--no-cpu-baseline]
 
 One step = one misfit + gradient call (forward sweep with boundary saving,
 residual, reverse / adjoint sweeps with imaging) over the workload's shots.
@@ -13,6 +14,9 @@ fwigb_misfit_grad_obs with pinned host buffers (model in, gradients out).
 `--impl reference` times the reference algorithm's CPU implementation (the
 oracle restatement, all host threads) on a bounded number of time steps of
 the same workload. With N > 1 (torchrun) every rank runs its own replica.
+Shots with their own aperture window and record length count their own
+cells and steps. `--compare-single` also times one step with one shot per
+launch (groups of one) on the same workload.
 """
 from __future__ import annotations
 
@@ -49,19 +53,60 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def workload(name, nsteps=None):
-    fw = ge.load_package()
+def workload(name, nsteps=None, shots=None):
+    ge.load_package()
     from fwiflow_gb300 import synthetic
 
     if name == "small_layered":
         return synthetic.small_layered(**({"nSteps": nsteps} if nsteps else {}))
+    if name == "batched_uneven":
+        kw = {"n_shots": shots or 64}
+        if nsteps:  # scale the record lengths down (profiler captures)
+            kw["steps"] = (max(2, nsteps * 3 // 8), nsteps)
+        return synthetic.batched_uneven(**kw)
     return synthetic.dipping_grf(**({"nSteps": nsteps} if nsteps else {}))
 
 
+def shot_sizes(w):
+    """(cells, steps) of every shot: its sub-grid (aperture window + 2 nPml
+    columns) and its record length."""
+    out = []
+    for s in w.shots:
+        nx = s["win_x1"] - s["win_x0"] + 1 + 2 * w.nPml if "win_x0" in s else w.nx_pad
+        out.append((w.nz_pad * nx, int(s.get("nSteps", w.nSteps))))
+    return out
+
+
+def sweep_cell_steps(w):
+    """Cell-steps each sweep kind processes in one misfit + gradient call:
+    forward stress / velocity and backward B run nSteps-1 times per shot,
+    backward C nSteps times."""
+    sz = shot_sizes(w)
+    fwd = sum(c * (n - 1) for c, n in sz)
+    return [fwd, fwd, fwd, sum(c * n for c, n in sz)]
+
+
 def describe(w):
+    sz = shot_sizes(w)
+    if w.name == "batched_uneven":
+        return (f"{w.name}: {w.nz}x{w.nx} interior + {w.nPml} CPML (nPad {w.nPad}); {len(w.shots)} shots, aperture "
+                f"windows {min(c for c, _ in sz) // w.nz_pad - 2 * w.nPml}..{max(c for c, _ in sz) // w.nz_pad - 2 * w.nPml}"
+                f" columns, record lengths {min(n for _, n in sz)}..{max(n for _, n in sz)} steps, Ricker 8-12 Hz, "
+                f"dx {w.dx} m, dt {w.dt * 1e3:g} ms, FP32; one misfit+gradient per step")
     return (f"{w.name}: {w.nz}x{w.nx} interior + {w.nPml} CPML (nPad {w.nPad}) = {w.nz_pad}x{w.nx_pad} cells, "
             f"{w.nSteps} steps, {len(w.shots)} shot(s), dx {w.dx} m, dt {w.dt * 1e3:g} ms, FP32; "
             f"one misfit+gradient per step")
+
+
+def store_gib(w):
+    """Boundary store streamed per call: 5 fields x the 5-layer ring of every
+    shot's sub-grid x its record length."""
+    tot = 0
+    for c, n in shot_sizes(w):
+        nx = c // w.nz_pad
+        ring = 10 * (nx - 2 * w.nPml + 4) + 10 * (w.nz_pad - 2 * w.nPml - w.nPad - 6)
+        tot += n * 5 * 4 * ring
+    return tot / 2 ** 30
 
 
 class ClockSampler:
@@ -130,7 +175,11 @@ def run_cpu_oracle(w, n_steps_sample, reps=1):
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
     from dataclasses import replace
 
-    ws = replace(w, nSteps=n_steps_sample, stf=np.ascontiguousarray(w.stf[:, :n_steps_sample]))
+    shots = [dict(s, nSteps=min(int(s.get("nSteps", n_steps_sample)), n_steps_sample)) for s in w.shots]
+    if any("win_x0" in s for s in w.shots):
+        shots = shots[:1]  # one windowed shot bounds the sample
+    ws = replace(w, nSteps=n_steps_sample, stf=np.ascontiguousarray(w.stf[:len(shots), :n_steps_sample]),
+                 shots=shots)
     tmp = tempfile.mkdtemp()
     para = ws.write_files(tmp)
     ids = list(range(len(ws.shots)))
@@ -143,7 +192,7 @@ def run_cpu_oracle(w, n_steps_sample, reps=1):
         orc.cufd(1, lam, mu, rho, ws.stf, ids, para, nthreads=nthreads)
         orc.cufd(0, lam, mu, rho, ws.stf, ids, para, nthreads=nthreads)
         times.append(time.perf_counter() - t0)
-    pts = ws.cells * n_steps_sample * len(ids)
+    pts = sum(c * n for c, n in shot_sizes(ws))
     return pts / min(times) / 1e9, times, nthreads
 
 
@@ -153,7 +202,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dipping_grf", choices=["dipping_grf", "small_layered"])
+    ap.add_argument("--workload", default="dipping_grf", choices=["dipping_grf", "small_layered", "batched_uneven"])
+    ap.add_argument("--shots", type=int, default=None, help="shots of the batched_uneven workload (default 64)")
+    ap.add_argument("--compare-single", action="store_true",
+                    help="also time one step with one shot per launch on the same workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-steps", type=int, default=3000)
     ap.add_argument("--nsteps", type=int, default=None,
@@ -163,13 +215,14 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    w = workload(args.workload, args.nsteps)
+    w = workload(args.workload, args.nsteps, args.shots)
     metric, unit = "fwd+adj Gpts/s vs HBM roofline", "Gpts/s"
+    cell_steps = sum(c * n for c, n in shot_sizes(w))
     cfg = {"workload": describe(w), "cells": w.cells, "nSteps": w.nSteps, "shots": len(w.shots),
+           "cell_steps_per_call": cell_steps,
            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
            "l2": "flushed between timed steps (256 MiB write); each step also streams a "
-                 f"{w.nSteps * 5 * 4 * (10 * (w.nx_pad - 2 * w.nPml + 4) + 10 * (w.nz_pad - 2 * w.nPml - w.nPad - 6)) / 2**30:.2f}"
-                 " GiB boundary store"}
+                 f"{store_gib(w):.2f} GiB boundary store"}
 
     if args.impl == "reference":
         if rank != 0:
@@ -248,7 +301,7 @@ def main():
         t = torch.tensor([dev_s, wall], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         dev_s, wall = float(t[0]), float(t[1])
-    pts_step = w.cells * w.nSteps * len(ids)
+    pts_step = cell_steps
     value = world * pts_step * args.steps / dev_s / 1e9
 
     # Per-kernel event timing (one instrumented step) for the roofline.
@@ -257,12 +310,15 @@ def main():
     tot, cnt = ctx.kernel_times()
     ctx.set_kernel_timing(False)
     k_dom = int(np.argmax(tot))
-    avg_s = tot[k_dom] / cnt[k_dom] / 1e3
     peak, peak_kind = peaks()
-    achieved = SWEEP_BYTES[k_dom] * w.cells / avg_s / 1e9
+    # Algorithmic bytes of a kind = bytes per cell-step x the cell-steps all
+    # its launches processed; per launch = that / launches (one shot: cells x bytes).
+    kcs = sweep_cell_steps(w)
+    kbytes = [SWEEP_BYTES[k] * kcs[k] for k in range(4)]
+    achieved = kbytes[k_dom] / (tot[k_dom] / 1e3) / 1e9
     per_kernel = {SWEEP_NAMES[k]: {"launches": int(cnt[k]), "avg_us": 1e3 * tot[k] / max(cnt[k], 1),
                                    "share": float(tot[k] / tot.sum()),
-                                   "algorithmic_GBps": SWEEP_BYTES[k] * w.cells / (tot[k] / max(cnt[k], 1) / 1e3) / 1e9}
+                                   "algorithmic_GBps": kbytes[k] / (tot[k] / 1e3) / 1e9}
                   for k in range(4)}
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "dram_traffic.txt")
@@ -270,7 +326,7 @@ def main():
         for line in open(tfile):
             parts = line.split()
             if len(parts) >= 3 and parts[0] == SWEEP_KERNELS[k_dom] and not line.startswith("#"):
-                traffic = float(parts[1]) * w.cells / float(parts[2])
+                traffic = float(parts[1]) * (kcs[k_dom] / max(cnt[k_dom], 1)) / float(parts[2])
     step_gbps = FWD_ADJ_BYTES * pts_step / (dev_s / args.steps) / 1e9
 
     # End to end through the public C ABI with pinned host buffers.
@@ -283,7 +339,7 @@ def main():
     stf_h = pinned(w.stf, torch.float64)
     obs_blk = np.zeros((len(ids), ctx.nrec_max, w.nSteps), dtype=np.float32)
     for i, o in enumerate(obs):
-        obs_blk[i, :o.shape[0]] = o
+        obs_blk[i, :o.shape[0], :o.shape[1]] = o
     obs_h = pinned(obs_blk, torch.float32)
     out = {k: pinned(np.zeros((w.nz_pad, w.nx_pad)), torch.float64) for k in ("gl", "gm", "gd")}
     gs_h = pinned(np.zeros((len(ids), w.nSteps)), torch.float64)
@@ -312,7 +368,28 @@ def main():
         e2e_s = float(t[0])
     e2e_val = world * pts_step * args.steps / e2e_s / 1e9
     h2d = 3 * w.cells * 8 + stf_h.nbytes + obs_h.nbytes
-    d2h = 3 * w.cells * 8 + len(ids) * w.nSteps * 4 + 8
+    d2h = 3 * w.cells * 8 + len(ids) * w.nSteps * 8 + 8
+
+    single = None
+    if args.compare_single:
+        # The same call with one shot per launch (groups of one shot).
+        ctx.set_model(lam, mu, rho)
+        ctx.stage_shots(w.stf, ids, obs=obs)
+        ctx.set_batching(max_shots=1)
+        ctx.run(1)
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+            ctx.run(1)
+            e1.record(stream)
+        ctx.synchronize()
+        torch.cuda.synchronize()
+        s_single = e0.elapsed_time(e1) / 1e3
+        ctx.set_batching(max_shots=0)
+        single = {"value": pts_step / s_single / 1e9, "unit": unit, "ms_per_step": 1e3 * s_single,
+                  "groups": ctx.last_group_count(), "note": "same call, one shot per launch"}
 
     if rank != 0:
         return
@@ -324,12 +401,14 @@ def main():
         "roofline": {"bound": "hbm", "kernel": SWEEP_KERNELS[k_dom], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback 6.8 TB/s",
-                     "traffic": traffic, "algorithmic_bytes_per_launch": SWEEP_BYTES[k_dom] * w.cells,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": kbytes[k_dom] / max(cnt[k_dom], 1),
                      "step_algorithmic_GBps": step_gbps, "step_frac": step_gbps / peak, "kernels": per_kernel},
         "e2e": {"value": e2e_val, "unit": unit, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": clk,
     }
+    if single:
+        line["one_shot_per_launch"] = single
     if not args.no_cpu_baseline:
         g, t, threads = run_cpu_oracle(w, min(args.cpu_sample_steps, w.nSteps))
         line["cpu_baseline"] = {"value": g, "unit": unit, "cores": threads, "kind": "port",

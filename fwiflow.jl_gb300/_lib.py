@@ -46,6 +46,7 @@ SIGNATURES = {
                               ctypes.c_int),
     "fwigb_geometry": ([_V, _I, _I, _I, _I, _I], ctypes.c_int),
     "fwigb_shot_nrec": ([_V, ctypes.c_int, _I], ctypes.c_int),
+    "fwigb_shot_info": ([_V, ctypes.c_int, _I, _I, _I, _I], ctypes.c_int),
     "fwigb_cufd": ([_D, _D, _D, _D, _D, _D, _D, _D, _D, ctypes.c_int, ctypes.c_int, ctypes.c_int, _I,
                     ctypes.c_char_p], ctypes.c_int),
     "fwigb_set_model": ([_V, _D, _D, _D], ctypes.c_int),
@@ -57,6 +58,8 @@ SIGNATURES = {
     "fwigb_last_launch_count": ([_V], ctypes.c_longlong),
     "fwigb_set_kernel_timing": ([_V, ctypes.c_int], ctypes.c_int),
     "fwigb_tile_config": ([_V, _I], ctypes.c_int),
+    "fwigb_set_batching": ([_V, ctypes.c_int, ctypes.c_ulonglong], ctypes.c_int),
+    "fwigb_last_group_count": ([_V], ctypes.c_int),
     "fwigb_set_tile_config": ([_V, _I], ctypes.c_int),
     "fwigb_kernel_times": ([_V, _D, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
 }

@@ -49,6 +49,13 @@ struct ShotGeom {
   int z_src = 0, x_src = 0;  // padded-grid cell (survey index + nPml, Src_Rec.cu:86,90)
   std::vector<int> z_rec, x_rec;
   std::vector<float> win_start, win_end, weights;
+  // Optional per-shot keys of this package (the reference's parser ignores
+  // them): record length "nSteps" (<= the parameter file's) and an aperture
+  // window "win_x0" .. "win_x1" of interior columns. The shot then runs on
+  // the sub-grid of padded columns win_x0 .. win_x1 + 2 nPml.
+  int nSteps = 0;
+  int x_off = 0;   // first padded column of the shot's sub-grid
+  int nx = 0;      // sub-grid width
 };
 
 // Parameter.cpp:16-178. Integer keys must be integers; dt, dz, dx, f0 any number.
@@ -168,6 +175,46 @@ static bool load_survey(const Params& p, std::vector<ShotGeom>& shots, int& nrec
       err = p.survey_fname + ": shot" + std::to_string(s) + " source too close to the grid edge";
       return false;
     }
+    g.nSteps = p.nSteps;
+    if (const JValue* v = d->get("nSteps")) {
+      g.nSteps = static_cast<int>(v->num);
+      if (v->kind != JValue::Number || g.nSteps < 2 || g.nSteps > p.nSteps) {
+        err = p.survey_fname + ": shot" + std::to_string(s) + " nSteps must be in [2, " + std::to_string(p.nSteps) +
+              "]";
+        return false;
+      }
+    }
+    g.x_off = 0;
+    g.nx = p.nx;
+    {
+      const JValue* a = d->get("win_x0");
+      const JValue* b = d->get("win_x1");
+      if ((a != nullptr) != (b != nullptr)) {
+        err = p.survey_fname + ": shot" + std::to_string(s) + " needs both win_x0 and win_x1";
+        return false;
+      }
+      if (a) {
+        const int w0 = static_cast<int>(a->num), w1 = static_cast<int>(b->num);
+        const int nxi = p.nx - 2 * p.nPml;
+        if (w0 < 0 || w1 >= nxi || w1 - w0 + 1 < 6) {
+          err = p.survey_fname + ": shot" + std::to_string(s) + " aperture window outside the interior or too narrow";
+          return false;
+        }
+        g.x_off = w0;
+        g.nx = w1 - w0 + 1 + 2 * p.nPml;
+      }
+    }
+    // Source and receivers must lie inside the shot's sub-grid (away from
+    // its edge by the reference's 9x9 source stencil).
+    if (g.x_src - g.x_off < 4 || g.x_src - g.x_off >= g.nx - 4) {
+      err = p.survey_fname + ": shot" + std::to_string(s) + " source outside its aperture window";
+      return false;
+    }
+    for (int r = 0; r < nrec; ++r)
+      if (g.x_rec[r] - g.x_off < 0 || g.x_rec[r] - g.x_off >= g.nx) {
+        err = p.survey_fname + ": shot" + std::to_string(s) + " receiver outside its aperture window";
+        return false;
+      }
     if (p.if_win) {
       const JValue* a = d->get("win_start");
       const JValue* b = d->get("win_end");
@@ -308,10 +355,23 @@ struct DevBuf {
   }
 };
 
-struct StagedShot {
-  int id;
-  int nrec;
-  ShotGeom* geom;
+
+
+// A staged shot: its survey geometry, its sub-grid and where its data sit in
+// the per-shot pools (offsets in elements).
+struct ShotPlan {
+  int id = 0;
+  const ShotGeom* geom = nullptr;
+  int nSteps = 0, nrec = 0, nx = 0, x_off = 0;
+  Geo g{};              // geometry of the shot's sub-grid
+  int nbin_z = 0, nbin = 0;
+  size_t src_off = 0;   // floats: 2 * nSteps (szz and sxx source terms)
+  size_t rec_off = 0;   // ints: 2 * nrec (sub-grid z, then x)
+  size_t blk_off = 0;   // ints: nbin + 1 + nrec (receiver bins, CSR)
+  size_t data_off = 0;  // floats: obs | syn | res, each nrec * nSteps
+  size_t taper_off = 0; // floats: 2 * nSteps, or 2 * nrec * nSteps with per-trace windows
+  size_t gstf_off = 0;  // floats: nSteps
+  size_t cpmlx_off = 0; // floats: 6 * nx (CPML x profiles of the sub-grid)
 };
 
 }  // namespace fwigb
@@ -326,41 +386,50 @@ struct fwigb_ctx {
   Params p;
   std::vector<ShotGeom> survey;
   int nrec_max = 0;
-  Geo geo{};
+  Geo geo{};  // full grid
   cudaStream_t stream = nullptr;
-  size_t cells = 0;   // allocated cells per grid array (ldz * nx)
-  size_t ncell = 0;   // logical cells (nz * nx), the size of host arrays
-  SweepMaps maps[3];  // tensor maps for tile widths 4, 8, 16
-  int tx[4] = {8, 8, 8, 8};  // tile width per sweep (F1, F2, B, C)
-  bool tuned_fwd = false, tuned_bwd = false;
-  bool autotune = true;
-  // device buffers
-  DevBuf media, stage, cpml, fields, grads, store, scal, partials;
-  DevBuf shot_src, shot_rec, shot_blk, shot_data, shot_taper, shot_gstf;
-  // staged shots
-  std::vector<StagedShot> staged;
+  size_t cells = 0;  // allocated cells of a full-grid array (ldz * nx)
+  size_t ncell = 0;  // logical cells (nz * nx), the size of host arrays
+  // Full-grid buffers: media, staging, CPML z profiles + full-width x
+  // profiles, global gradients, scalars, reduction partials.
+  DevBuf media, stage, cpml, grads, scal, partials;
+  // Staged shots and their data.
+  std::vector<ShotPlan> plans;
+  DevBuf shot_src, shot_rec, shot_blk, shot_data, shot_taper, shot_gstf, shot_cpmlx;
   bool with_obs = false;
   bool per_trace_taper = false;
-  int nblk = 0;  // receiver bins (32 x 8 cells)
-  int nbin_z = 0;
+  int nSteps_max = 0;  // longest staged record
+  // Shot groups run concurrently; group state is per member slot.
+  int max_batch = 0;      // cap on shots per group (0: memory budget only)
+  size_t mem_budget = 0;  // bytes for group state (0: 90% of free device memory)
+  size_t fields_stride = 0, store_stride = 0, grads_stride = 0;  // floats per member
+  DevBuf g_fields, g_store, g_grads, g_slots;
+  int group_cap = 0;
+  // Launch parameter packs of the current group: for a lone shot one
+  // SweepPack<1> per (sweep, tile width); else one SweepPack<kPackShots> per
+  // (sweep, tile width, pack of consecutive members), index
+  // (sweep * 3 + tile slot) * npacks + pack. pack_nx[q] is the widest member
+  // sub-grid of pack q.
+  int group_size = 0, npacks = 0;
+  std::vector<SweepPack<1>> pack1;
+  std::vector<SweepPack<kPackShots>> packs;
+  std::vector<int> pack_nx;
+  int last_groups = 0;
   bool model_set = false;
   int last_calc = -1;
   long long launches = 0;
+  int tx[4] = {8, 8, 8, 8};  // tile width per sweep (F1, F2, B, C)
+  bool tuned_fwd = false, tuned_bwd = false;
+  bool autotune = true;
   // per-kernel event timing
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
-  std::vector<int> ev_kind;  // kind of the i-th event pair of the last run
+  std::vector<int> ev_kind;
 };
 
 namespace {
 
 thread_local std::string g_err;
-
-#define TRY_RC(call)                  \
-  do {                                \
-    int rc_ = (call);                 \
-    if (rc_ != FWIGB_OK) return rc_;  \
-  } while (0)
 
 #define CK(call)                                                                                   \
   do {                                                                                             \
@@ -371,22 +440,17 @@ thread_local std::string g_err;
     }                                                                                              \
   } while (0)
 
+#define TRY_RC(call)                 \
+  do {                               \
+    int rc_ = (call);                \
+    if (rc_ != FWIGB_OK) return rc_; \
+  } while (0)
+
 int tx_slot(int tx) { return tx == 4 ? 0 : (tx == 8 ? 1 : 2); }
 
-Fields fields_of(fwigb_ctx* ctx) {
-  float* b = ctx->fields.as<float>();
-  const size_t n = ctx->cells;
-  Fields f;
-  float** slots[18] = {&f.vz,       &f.vx,       &f.szz,      &f.sxx,      &f.sxz,       &f.vz_a,
-                       &f.vx_a,     &f.szz_a,    &f.sxx_a,    &f.sxz_a,    &f.m_dvz_dz,  &f.m_dvz_dx,
-                       &f.m_dvx_dz, &f.m_dvx_dx, &f.m_dszz_dz, &f.m_dsxx_dx, &f.m_dsxz_dz, &f.m_dsxz_dx};
-  for (int k = 0; k < 18; ++k) *slots[k] = b + k * n;
-  return f;
-}
-
-// media: lam, mu, den, l2m, aveMu, bycA, bycB, hs, muw
-MediaD media_of(fwigb_ctx* ctx) {
-  float* b = ctx->media.as<float>();
+// Media slots: lam, mu, den, l2m, aveMu, bycA, bycB, hs, muw (full grid).
+MediaD media_view(fwigb_ctx* ctx, int x_off) {
+  float* b = ctx->media.as<float>() + static_cast<size_t>(x_off) * ctx->geo.ldz;
   const size_t n = ctx->cells;
   MediaD m;
   m.lam = b;
@@ -399,66 +463,36 @@ MediaD media_of(fwigb_ctx* ctx) {
   return m;
 }
 
-CpmlD cpml_of(fwigb_ctx* ctx) {
-  const float* b = ctx->cpml.as<float>();
-  const int nz = ctx->p.nz, nx = ctx->p.nx;
-  CpmlD c;
-  c.K_z = b;
-  c.a_z = b + nz;
-  c.b_z = b + 2 * nz;
-  c.K_zh = b + 3 * nz;
-  c.a_zh = b + 4 * nz;
-  c.b_zh = b + 5 * nz;
-  const float* x = b + 6 * nz;
-  c.K_x = x;
-  c.a_x = x + nx;
-  c.b_x = x + 2 * nx;
-  c.K_xh = x + 3 * nx;
-  c.a_xh = x + 4 * nx;
-  c.b_xh = x + 5 * nx;
-  return c;
-}
-
-int setup_geometry(fwigb_ctx* ctx) {
-  const Params& p = ctx->p;
-  Geo& g = ctx->geo;
+// Geometry of a grid of width nx (the full grid or a shot's sub-grid) with
+// the CPML profiles az/azh (z) and ax/axh (x) of that grid.
+Geo make_geo(const Params& p, int nx, const float* az, const float* azh, const float* ax, const float* axh) {
+  Geo g{};
   g.nz = p.nz;
-  g.nx = p.nx;
+  g.nx = nx;
   g.ldz = (p.nz + 31) / 32 * 32;
   g.nPml = p.nPml;
   g.nPad = p.nPad;
   g.zs0 = 2;
   g.zs1 = p.nz - p.nPad - 3;
   g.xs0 = 2;
-  g.xs1 = p.nx - 3;
+  g.xs1 = nx - 3;
   g.zi0 = p.nPml;
   g.zi1 = p.nz - p.nPad - 1 - p.nPml;
   g.xi0 = p.nPml;
-  g.xi1 = p.nx - 1 - p.nPml;
+  g.xi1 = nx - 1 - p.nPml;
   g.zpml_hi = p.nz - p.nPml - p.nPad - 1;
-  g.xpml_hi_s = p.nx - p.nPml - 1;
-  g.xpml_hi_v = p.nx - p.nPml;
+  g.xpml_hi_s = nx - p.nPml - 1;
+  g.xpml_hi_v = nx - p.nPml;
   g.rz0 = p.nPml - 2;
   g.rz1 = p.nz - p.nPml - p.nPad + 1;
   g.rx0 = p.nPml - 2;
-  g.rx1 = p.nx - p.nPml + 1;
+  g.rx1 = nx - p.nPml + 1;
   g.ringW = g.rx1 - g.rx0 + 1;
   g.ringH = g.rz1 - g.rz0 + 1 - 10;
   g.ring_len = 10 * g.ringW + 10 * g.ringH;
   g.dt = p.dt;
   g.rdz = 1.0f / p.dz;
   g.rdx = 1.0f / p.dx;
-  ctx->cells = static_cast<size_t>(g.ldz) * p.nx;
-  ctx->ncell = static_cast<size_t>(p.nz) * p.nx;
-
-  // CPML profiles (host) and the adjoint-memory bands derived from them.
-  std::vector<float> h(6 * p.nz + 6 * p.nx);
-  float* z = h.data();
-  float* x = h.data() + 6 * p.nz;
-  cpml_profile(p.nz - p.nPad, p.nz, p.nPml, p.dz, p.f0, p.dt, z, z + p.nz, z + 2 * p.nz, z + 3 * p.nz, z + 4 * p.nz,
-               z + 5 * p.nz);
-  cpml_profile(p.nx, p.nx, p.nPml, p.dx, p.f0, p.dt, x, x + p.nx, x + 2 * p.nx, x + 3 * p.nx, x + 4 * p.nx,
-               x + 5 * p.nx);
   // An adjoint psi memory cell matters only within 2 cells of a cell whose
   // CPML coefficient a (or a_half) is non-zero; elsewhere the reference's
   // updates (el_stress_adj.cu:68-94) are multiplied by a == 0.
@@ -470,31 +504,35 @@ int setup_geometry(fwigb_ctx* ctx) {
     for (int i = n - 1; i >= n / 2; --i)
       if (a[i] != 0.0f || ah[i] != 0.0f) hi = i - 2;
   };
-  band(z + p.nz, z + 4 * p.nz, p.nz - p.nPad, g.zband_lo, g.zband_hi);
-  band(x + p.nx, x + 4 * p.nx, p.nx, g.xband_lo, g.xband_hi);
+  band(az, azh, p.nz - p.nPad, g.zband_lo, g.zband_hi);
+  band(ax, axh, nx, g.xband_lo, g.xband_hi);
+  return g;
+}
+
+int setup_geometry(fwigb_ctx* ctx) {
+  const Params& p = ctx->p;
+  // CPML profiles: z (length nz, profile over nz - nPad, Cpml.cu:46-48) and x
+  // of the full width; shots with an aperture window get their own x profiles.
+  std::vector<float> h(6 * p.nz + 6 * p.nx);
+  float* z = h.data();
+  float* x = h.data() + 6 * p.nz;
+  cpml_profile(p.nz - p.nPad, p.nz, p.nPml, p.dz, p.f0, p.dt, z, z + p.nz, z + 2 * p.nz, z + 3 * p.nz, z + 4 * p.nz,
+               z + 5 * p.nz);
+  cpml_profile(p.nx, p.nx, p.nPml, p.dx, p.f0, p.dt, x, x + p.nx, x + 2 * p.nx, x + 3 * p.nx, x + 4 * p.nx,
+               x + 5 * p.nx);
+  ctx->geo = make_geo(p, p.nx, z + p.nz, z + 4 * p.nz, x + p.nx, x + 4 * p.nx);
+  ctx->cells = static_cast<size_t>(ctx->geo.ldz) * p.nx;
+  ctx->ncell = static_cast<size_t>(p.nz) * p.nx;
   CK(ctx->cpml.ensure(h.size() * sizeof(float)));
   CK(cudaMemcpy(ctx->cpml.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
   CK(ctx->media.ensure(9 * ctx->cells * sizeof(float)));
+  CK(cudaMemset(ctx->media.p, 0, 9 * ctx->cells * sizeof(float)));
   CK(ctx->stage.ensure(3 * ctx->ncell * sizeof(double)));
-  CK(ctx->fields.ensure(18 * ctx->cells * sizeof(float)));
   CK(ctx->grads.ensure(3 * ctx->cells * sizeof(float)));
   // [0]: misfit accumulator (double), [8]: cp max bits, [16]: sweep error word
   CK(ctx->scal.ensure(64));
   CK(cudaMemset(ctx->scal.p, 0, 64));
-  // Padding rows (ldz > nz) and every field start at zero.
-  CK(cudaMemset(ctx->media.p, 0, 9 * ctx->cells * sizeof(float)));
-  CK(cudaMemset(ctx->fields.p, 0, 18 * ctx->cells * sizeof(float)));
   CK(ctx->partials.ensure(1024 * sizeof(double)));
-  ctx->nbin_z = (p.nz + kBinZ - 1) / kBinZ;
-  ctx->nblk = ctx->nbin_z * ((p.nx + kBinX - 1) / kBinX);
-  const Fields f = fields_of(ctx);
-  for (int k = 0; k < 3; ++k) {
-    const char* why = nullptr;
-    if (!encode_sweep_maps(g, f, kTileXs[k], ctx->maps[k], &why)) {
-      ctx->err = why;
-      return FWIGB_ERR_CUDA;
-    }
-  }
   return FWIGB_OK;
 }
 
@@ -566,10 +604,11 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
     return FWIGB_ERR_UNSUPPORTED;
   }
   CK(cudaSetDevice(ctx->device));
-  const int nt = p.nSteps, nrm = ctx->nrec_max;
-  ctx->staged.clear();
-  for (int i = 0; i < n_shots; ++i) {
-    const int id = shot_ids[i];
+  const int nt_max = p.nSteps, nrm = ctx->nrec_max;
+  ctx->plans.clear();
+  size_t n_src = 0, n_rec = 0, n_blk = 0, n_data = 0, n_taper = 0, n_gstf = 0, n_cpmlx = 0;
+  for (int k = 0; k < n_shots; ++k) {
+    const int id = shot_ids[k];
     if (id < 0 || id >= static_cast<int>(ctx->survey.size()) || !ctx->survey[id].present) {
       ctx->err = "shot id " + std::to_string(id) + " not in the survey file";
       return FWIGB_ERR_ARG;
@@ -578,143 +617,319 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
       ctx->err = "shot id " + std::to_string(id) + " has no stf row";
       return FWIGB_ERR_ARG;
     }
-    ctx->staged.push_back({id, static_cast<int>(ctx->survey[id].z_rec.size()), &ctx->survey[id]});
+    const ShotGeom& sg = ctx->survey[id];
+    ShotPlan pl;
+    pl.id = id;
+    pl.geom = &sg;
+    pl.nSteps = sg.nSteps;
+    pl.nrec = static_cast<int>(sg.z_rec.size());
+    pl.nx = sg.nx;
+    pl.x_off = sg.x_off;
+    pl.nbin_z = (p.nz + kBinZ - 1) / kBinZ;
+    pl.nbin = pl.nbin_z * ((pl.nx + kBinX - 1) / kBinX);
+    pl.src_off = n_src;
+    n_src += 2 * static_cast<size_t>(pl.nSteps);
+    pl.rec_off = n_rec;
+    n_rec += 2 * static_cast<size_t>(pl.nrec);
+    pl.blk_off = n_blk;
+    n_blk += static_cast<size_t>(pl.nbin) + 1 + pl.nrec;
+    pl.data_off = n_data;
+    n_data += 3 * static_cast<size_t>(pl.nrec) * pl.nSteps;
+    pl.taper_off = n_taper;
+    n_taper += 2 * static_cast<size_t>(pl.nSteps) * (p.if_win ? pl.nrec : 1);
+    pl.gstf_off = n_gstf;
+    n_gstf += static_cast<size_t>(pl.nSteps);
+    pl.cpmlx_off = n_cpmlx;
+    n_cpmlx += 6 * static_cast<size_t>(pl.nx);
+    ctx->plans.push_back(pl);
   }
-  const size_t ns = ctx->staged.size();
-  // Sources: taper 0.001 (Src_Rec.cu:140) and the add_source scale (utilities.cu:528-538).
-  std::vector<float> hsrc(2 * ns * nt);
-  std::vector<float> w(nt);
-  if (!taper_weights(nt, p.dt, 0.001f, w.data())) {
-    ctx->err = "nSteps too small for the source taper";
-    return FWIGB_ERR_ARG;
-  }
-  const float scale = 2250000.0f;  // pow(1500.0, 2)
-  for (size_t s = 0; s < ns; ++s) {
-    const double* row = stf + static_cast<size_t>(ctx->staged[s].id) * nt;
+  std::vector<float> hsrc(n_src), htaper(n_taper, 1.0f), hcpml(n_cpmlx);
+  std::vector<int> hrec(n_rec), hblk(n_blk, 0);
+  const float* zprof = nullptr;
+  std::vector<float> zh(6 * p.nz);
+  cpml_profile(p.nz - p.nPad, p.nz, p.nPml, p.dz, p.f0, p.dt, zh.data(), zh.data() + p.nz, zh.data() + 2 * p.nz,
+               zh.data() + 3 * p.nz, zh.data() + 4 * p.nz, zh.data() + 5 * p.nz);
+  zprof = zh.data();
+  const float scale = 2250000.0f;  // pow(1500.0, 2) (utilities.cu:528)
+  ctx->nSteps_max = 0;
+  for (ShotPlan& pl : ctx->plans) {
+    const int nt = pl.nSteps;
+    ctx->nSteps_max = std::max(ctx->nSteps_max, nt);
+    // CPML x profiles of the sub-grid and its geometry.
+    float* x = hcpml.data() + pl.cpmlx_off;
+    cpml_profile(pl.nx, pl.nx, p.nPml, p.dx, p.f0, p.dt, x, x + pl.nx, x + 2 * pl.nx, x + 3 * pl.nx, x + 4 * pl.nx,
+                 x + 5 * pl.nx);
+    pl.g = make_geo(p, pl.nx, zprof + p.nz, zprof + 4 * p.nz, x + pl.nx, x + 4 * pl.nx);
+    // Source: taper 0.001 (Src_Rec.cu:140) and the add_source scale (utilities.cu:528-538).
+    std::vector<float> w(nt);
+    if (!taper_weights(nt, p.dt, 0.001f, w.data())) {
+      ctx->err = "nSteps too small for the source taper";
+      return FWIGB_ERR_ARG;
+    }
+    const double* row = stf + static_cast<size_t>(pl.id) * nt_max;
     for (int it = 0; it < nt; ++it) {
       const float amp = static_cast<float>(row[it]) * w[it];
-      hsrc[(2 * s) * nt + it] = scale * amp * p.dt;
-      hsrc[(2 * s + 1) * nt + it] = static_cast<float>(3.0 * scale * amp * p.dt);
+      hsrc[pl.src_off + it] = scale * amp * p.dt;
+      hsrc[pl.src_off + nt + it] = static_cast<float>(3.0 * scale * amp * p.dt);
     }
-  }
-  CK(ctx->shot_src.ensure(hsrc.size() * sizeof(float)));
-  CK(cudaMemcpyAsync(ctx->shot_src.p, hsrc.data(), hsrc.size() * sizeof(float), cudaMemcpyHostToDevice,
-                     ctx->stream));
-  // Receivers and their per-block lists (CSR over the sweep grid).
-  const int nbz = ctx->nbin_z;
-  const int nblk = ctx->nblk;
-  std::vector<int> hrec(2 * ns * nrm, 0), hblk(ns * (nblk + 1 + nrm), 0);
-  for (size_t s = 0; s < ns; ++s) {
-    const ShotGeom& g = *ctx->staged[s].geom;
-    const int nrec = ctx->staged[s].nrec;
-    int* rz = hrec.data() + 2 * s * nrm;
-    int* rx = rz + nrm;
-    int* off = hblk.data() + s * (nblk + 1 + nrm);
-    int* lst = off + nblk + 1;
-    std::vector<int> cnt(nblk + 1, 0);
-    for (int r = 0; r < nrec; ++r) {
+    // Receivers (sub-grid coordinates) and their 32 x 8 bins.
+    const ShotGeom& g = *pl.geom;
+    int* rz = hrec.data() + pl.rec_off;
+    int* rx = rz + pl.nrec;
+    int* off = hblk.data() + pl.blk_off;
+    int* lst = off + pl.nbin + 1;
+    std::vector<int> cnt(pl.nbin + 1, 0);
+    for (int r = 0; r < pl.nrec; ++r) {
       rz[r] = g.z_rec[r];
-      rx[r] = g.x_rec[r];
-      cnt[(g.z_rec[r] / kBinZ) + (g.x_rec[r] / kBinX) * nbz + 1]++;
+      rx[r] = g.x_rec[r] - pl.x_off;
+      cnt[(rz[r] / kBinZ) + (rx[r] / kBinX) * pl.nbin_z + 1]++;
     }
-    for (int b = 0; b < nblk; ++b) cnt[b + 1] += cnt[b];
-    for (int b = 0; b <= nblk; ++b) off[b] = cnt[b];
+    for (int b = 0; b < pl.nbin; ++b) cnt[b + 1] += cnt[b];
+    for (int b = 0; b <= pl.nbin; ++b) off[b] = cnt[b];
     std::vector<int> pos(cnt.begin(), cnt.end() - 1);
-    for (int r = 0; r < nrec; ++r) lst[pos[(g.z_rec[r] / kBinZ) + (g.x_rec[r] / kBinX) * nbz]++] = r;
+    for (int r = 0; r < pl.nrec; ++r) lst[pos[(rz[r] / kBinZ) + (rx[r] / kBinX) * pl.nbin_z]++] = r;
+    // Taper weights of the data and of the adjoint source.
+    float* tw = htaper.data() + pl.taper_off;
+    if (!p.if_win) {
+      if (!taper_weights(nt, p.dt, 0.005f, tw)) {
+        ctx->err = "nSteps too small for the data taper";
+        return FWIGB_ERR_ARG;
+      }
+      std::copy(tw, tw + nt, tw + nt);
+    } else {
+      const size_t per = static_cast<size_t>(pl.nrec) * nt;
+      for (int r = 0; r < pl.nrec; ++r) {
+        taper_weights_windowed(nt, p.dt, 0.005f, g.win_start[r], g.win_end[r], g.weights[r], tw + r * nt);
+        taper_weights_windowed(nt, p.dt, 0.1f, g.win_start[r], g.win_end[r], g.weights[r], tw + per + r * nt);
+      }
+    }
   }
-  CK(ctx->shot_rec.ensure(hrec.size() * sizeof(int)));
-  CK(ctx->shot_blk.ensure(hblk.size() * sizeof(int)));
-  CK(cudaMemcpyAsync(ctx->shot_rec.p, hrec.data(), hrec.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->shot_blk.p, hblk.data(), hblk.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-  // Data buffers: obs | syn | res, each [ns][nrec_max][nSteps].
-  const size_t per = static_cast<size_t>(nrm) * nt;
-  CK(ctx->shot_data.ensure(3 * ns * per * sizeof(float)));
+  ctx->per_trace_taper = p.if_win;
+  CK(ctx->shot_src.ensure(std::max<size_t>(n_src, 1) * sizeof(float)));
+  CK(ctx->shot_rec.ensure(std::max<size_t>(n_rec, 1) * sizeof(int)));
+  CK(ctx->shot_blk.ensure(std::max<size_t>(n_blk, 1) * sizeof(int)));
+  CK(ctx->shot_data.ensure(std::max<size_t>(n_data, 1) * sizeof(float)));
+  CK(ctx->shot_taper.ensure(std::max<size_t>(n_taper, 1) * sizeof(float)));
+  CK(ctx->shot_gstf.ensure(std::max<size_t>(n_gstf, 1) * sizeof(float)));
+  CK(ctx->shot_cpmlx.ensure(std::max<size_t>(n_cpmlx, 1) * sizeof(float)));
+  cudaStream_t s = ctx->stream;
+  CK(cudaMemcpyAsync(ctx->shot_src.p, hsrc.data(), n_src * sizeof(float), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ctx->shot_rec.p, hrec.data(), n_rec * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ctx->shot_blk.p, hblk.data(), n_blk * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ctx->shot_taper.p, htaper.data(), n_taper * sizeof(float), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ctx->shot_cpmlx.p, hcpml.data(), n_cpmlx * sizeof(float), cudaMemcpyHostToDevice, s));
   ctx->with_obs = with_obs;
   if (with_obs) {
-    float* d_obs = ctx->shot_data.as<float>();
-    if (obs) {
-      CK(cudaMemcpyAsync(d_obs, obs, ns * per * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
-    } else {
-      // libCUFD.cu:189-200: data_dir_name/Shot<id>.bin, [nrec][nSteps] float.
-      std::vector<float> buf(per);
-      for (size_t s = 0; s < ns; ++s) {
-        const std::string fn = p.data_dir_name + "/Shot" + std::to_string(ctx->staged[s].id) + ".bin";
+    // Observed data: from memory ([n_shots][nrec_max][nSteps] with shot k's
+    // [nrec][nSteps_k] block in its top-left corner) or from
+    // data_dir_name/Shot<id>.bin ([nrec][nSteps_k] float, libCUFD.cu:189-200).
+    std::vector<float> buf;
+    for (size_t k = 0; k < ctx->plans.size(); ++k) {
+      const ShotPlan& pl = ctx->plans[k];
+      float* d_obs = ctx->shot_data.as<float>(pl.data_off);
+      if (obs) {
+        CK(cudaMemcpy2DAsync(d_obs, pl.nSteps * sizeof(float), obs + k * static_cast<size_t>(nrm) * nt_max,
+                             nt_max * sizeof(float), pl.nSteps * sizeof(float), pl.nrec, cudaMemcpyHostToDevice, s));
+      } else {
+        const std::string fn = p.data_dir_name + "/Shot" + std::to_string(pl.id) + ".bin";
         std::FILE* fp = std::fopen(fn.c_str(), "rb");
         if (!fp) {
           ctx->err = "cannot read " + fn;
           return FWIGB_ERR_IO;
         }
-        const size_t want = static_cast<size_t>(ctx->staged[s].nrec) * nt;
+        const size_t want = static_cast<size_t>(pl.nrec) * pl.nSteps;
+        buf.resize(want);
         const size_t got = std::fread(buf.data(), sizeof(float), want, fp);
         std::fclose(fp);
         if (got != want) {
           ctx->err = fn + " is shorter than nrec*nSteps";
           return FWIGB_ERR_IO;
         }
-        CK(cudaMemcpy(d_obs + s * per, buf.data(), want * sizeof(float), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_obs, buf.data(), want * sizeof(float), cudaMemcpyHostToDevice));
       }
     }
   }
-  // Taper weights: [2][nt] shared, or per trace [ns][2][nrec_max][nt] with windows.
-  ctx->per_trace_taper = p.if_win;
-  std::vector<float> ht;
-  if (!p.if_win) {
-    ht.resize(2 * nt);
-    if (!taper_weights(nt, p.dt, 0.005f, ht.data())) {
-      ctx->err = "nSteps too small for the data taper";
-      return FWIGB_ERR_ARG;
-    }
-    std::copy(ht.begin(), ht.begin() + nt, ht.begin() + nt);
-  } else {
-    ht.assign(ns * 2 * per, 1.0f);
-    for (size_t s = 0; s < ns; ++s) {
-      const ShotGeom& g = *ctx->staged[s].geom;
-      for (int r = 0; r < ctx->staged[s].nrec; ++r) {
-        taper_weights_windowed(nt, p.dt, 0.005f, g.win_start[r], g.win_end[r], g.weights[r],
-                               ht.data() + (2 * s) * per + static_cast<size_t>(r) * nt);
-        taper_weights_windowed(nt, p.dt, 0.1f, g.win_start[r], g.win_end[r], g.weights[r],
-                               ht.data() + (2 * s + 1) * per + static_cast<size_t>(r) * nt);
-      }
-    }
-  }
-  CK(ctx->shot_taper.ensure(ht.size() * sizeof(float)));
-  CK(cudaMemcpyAsync(ctx->shot_taper.p, ht.data(), ht.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx->shot_gstf.ensure(ns * nt * sizeof(float)));
-  CK(cudaStreamSynchronize(ctx->stream));  // host staging vectors go out of scope
+  CK(cudaStreamSynchronize(s));  // host staging vectors go out of scope
   return FWIGB_OK;
 }
 
-// Tile-width autotuner: times every width of each sweep on this context's grid
-// (a few launches each on the live buffers, which the run then resets) and
-// keeps the fastest. Forward sweeps are tuned on the first run, backward sweeps
-// on the first run with the adjoint.
-int autotune(fwigb_ctx* ctx, const ShotD& sh, bool adj) {
+// Shot groups for one run: shots sorted by record length (longest first) and
+// cut into groups of at most group_cap members, which run concurrently.
+// group_cap follows the device-memory budget of the group state (fields,
+// gradients and, with the adjoint, the boundary store of every member).
+int plan_groups(fwigb_ctx* ctx, bool adj, std::vector<std::vector<int>>& groups) {
+  const Params& p = ctx->p;
+  int nx_max = 0, ring_max = 0;
+  for (const ShotPlan& pl : ctx->plans) {
+    nx_max = std::max(nx_max, pl.nx);
+    ring_max = std::max(ring_max, pl.g.ring_len);
+  }
+  const size_t ldz = ctx->geo.ldz;
+  ctx->fields_stride = 18 * ldz * nx_max;
+  ctx->grads_stride = 3 * ldz * nx_max;
+  ctx->store_stride = adj ? static_cast<size_t>(ctx->nSteps_max) * 5 * ring_max : 0;
+  const size_t per_member = (ctx->fields_stride + ctx->grads_stride + ctx->store_stride) * sizeof(float);
+  size_t budget = ctx->mem_budget;
+  if (!budget) {
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    // Memory the group state already holds is reusable.
+    free_b += ctx->g_fields.bytes + ctx->g_grads.bytes + ctx->g_store.bytes;
+    budget = static_cast<size_t>(0.9 * static_cast<double>(free_b));
+  }
+  int cap = static_cast<int>(std::min<size_t>(budget / std::max<size_t>(per_member, 1), 1u << 16));
+  if (ctx->max_batch > 0) cap = std::min(cap, ctx->max_batch);
+  cap = std::min(cap, static_cast<int>(ctx->plans.size()));
+  if (cap < 1) {
+    ctx->err = "one shot's wavefields and boundary store do not fit in device memory";
+    return FWIGB_ERR_OOM;
+  }
+  std::vector<int> order(ctx->plans.size());
+  for (size_t k = 0; k < order.size(); ++k) order[k] = static_cast<int>(k);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return ctx->plans[a].nSteps > ctx->plans[b].nSteps; });
+  groups.clear();
+  for (size_t k = 0; k < order.size(); k += cap)
+    groups.emplace_back(order.begin() + k, order.begin() + std::min(order.size(), k + cap));
+  ctx->group_cap = cap;
+  (void)p;
+  CK(ctx->g_fields.ensure(static_cast<size_t>(cap) * ctx->fields_stride * sizeof(float)));
+  CK(ctx->g_grads.ensure(static_cast<size_t>(cap) * ctx->grads_stride * sizeof(float)));
+  if (adj) CK(ctx->g_store.ensure(static_cast<size_t>(cap) * ctx->store_stride * sizeof(float)));
+  CK(ctx->g_slots.ensure(static_cast<size_t>(cap) * sizeof(ShotSlot)));
+  return FWIGB_OK;
+}
+
+// Launches sweep `w` (0 F1, 1 F2, 2 B, 3 C) over the first `a` members of
+// the current group at tile width tx, one launch per parameter pack; `arg`
+// is the step (F1) or the backward iteration (B, C). Returns the number of
+// launches.
+int launch_sweep(fwigb_ctx* ctx, int w, int tx, int a, int arg, bool save, unsigned* d_err) {
   cudaStream_t s = ctx->stream;
-  const Geo& g = ctx->geo;
-  Fields f = fields_of(ctx);
-  MediaD m = media_of(ctx);
-  CpmlD c = cpml_of(ctx);
-  StoreD st{ctx->store.as<float>()};
-  float* gb = ctx->grads.as<float>();
-  Grads gr{gb, gb + ctx->cells, gb + 2 * ctx->cells};
+  const int nz = ctx->p.nz;
+  const size_t base = static_cast<size_t>(w * 3 + tx_slot(tx));
+  auto go = [&](const auto& pk, int n, int nx) {
+    switch (w) {
+      case 0: launch_fwd_stress(s, tx, pk, n, nz, nx, arg, save, d_err); break;
+      case 1: launch_fwd_velocity(s, tx, pk, n, nz, nx, d_err); break;
+      case 2: launch_bwd_B(s, tx, pk, n, nz, nx, arg, d_err); break;
+      default: launch_bwd_C(s, tx, pk, n, nz, nx, arg, d_err); break;
+    }
+  };
+  if (a <= 0) return 0;
+  if (ctx->group_size == 1) {
+    go(ctx->pack1[base], 1, ctx->pack_nx[0]);
+    return 1;
+  }
+  int n = 0;
+  for (int q = 0; q * kPackShots < a; ++q, ++n)
+    go(ctx->packs[base * ctx->npacks + q], std::min(kPackShots, a - q * kPackShots), ctx->pack_nx[q]);
+  return n;
+}
+
+// Builds and uploads the slots and tensor maps of a group's members.
+int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
+  const size_t ldz = ctx->geo.ldz;
+  std::vector<ShotSlot> slots(members.size());
+  std::vector<TileMaps> maps(static_cast<size_t>(4 * 3) * ctx->group_cap);
+  const int nrm = 0;
+  (void)nrm;
+  nx_max = 0;
+  const float* cz = ctx->cpml.as<float>();
+  const int nz = ctx->p.nz;
+  for (size_t k = 0; k < members.size(); ++k) {
+    const ShotPlan& pl = ctx->plans[members[k]];
+    nx_max = std::max(nx_max, pl.nx);
+    ShotSlot& sl = slots[k];
+    sl.g = pl.g;
+    const size_t n = ldz * pl.nx;
+    float* fb = ctx->g_fields.as<float>(k * ctx->fields_stride);
+    float** f[18] = {&sl.f.vz,       &sl.f.vx,       &sl.f.szz,       &sl.f.sxx,       &sl.f.sxz,
+                     &sl.f.vz_a,     &sl.f.vx_a,     &sl.f.szz_a,     &sl.f.sxx_a,     &sl.f.sxz_a,
+                     &sl.f.m_dvz_dz, &sl.f.m_dvz_dx, &sl.f.m_dvx_dz,  &sl.f.m_dvx_dx,  &sl.f.m_dszz_dz,
+                     &sl.f.m_dsxx_dx, &sl.f.m_dsxz_dz, &sl.f.m_dsxz_dx};
+    for (int q = 0; q < 18; ++q) *f[q] = fb + q * n;
+    sl.m = media_view(ctx, pl.x_off);
+    const float* cx = ctx->shot_cpmlx.as<float>(pl.cpmlx_off);
+    sl.c = CpmlD{cz,      cz + nz,      cz + 2 * nz,      cz + 3 * nz,      cz + 4 * nz,      cz + 5 * nz,
+                 cx,      cx + pl.nx,   cx + 2 * pl.nx,   cx + 3 * pl.nx,   cx + 4 * pl.nx,   cx + 5 * pl.nx};
+    ShotD& sh = sl.sh;
+    sh.src_z = pl.geom->z_src;
+    sh.src_x = pl.geom->x_src - pl.x_off;
+    sh.src_szz = ctx->shot_src.as<float>(pl.src_off);
+    sh.src_sxx = sh.src_szz + pl.nSteps;
+    sh.nrec = pl.nrec;
+    sh.nSteps = pl.nSteps;
+    sh.rec_z = ctx->shot_rec.as<int>(pl.rec_off);
+    sh.rec_x = sh.rec_z + pl.nrec;
+    sh.blk_off = ctx->shot_blk.as<int>(pl.blk_off);
+    sh.blk_rec = sh.blk_off + pl.nbin + 1;
+    sh.nbin_z = pl.nbin_z;
+    const size_t per = static_cast<size_t>(pl.nrec) * pl.nSteps;
+    sh.data = ctx->shot_data.as<float>(pl.data_off + per);
+    sh.res = ctx->shot_data.as<float>(pl.data_off + 2 * per);
+    sh.gstf = ctx->shot_gstf.as<float>(pl.gstf_off);
+    sl.st = StoreD{ctx->store_stride ? ctx->g_store.as<float>(k * ctx->store_stride) : nullptr};
+    float* gb = ctx->g_grads.as<float>(k * ctx->grads_stride);
+    sl.gr = Grads{gb, gb + n, gb + 2 * n};
+    sl.nSteps = pl.nSteps;
+    sl.x_off = pl.x_off;
+    for (int t = 0; t < 3; ++t) {
+      SweepMaps sm{};
+      const char* why = nullptr;
+      if (!encode_sweep_maps(pl.g, sl.f, kTileXs[t], sm, &why)) {
+        ctx->err = why;
+        return FWIGB_ERR_CUDA;
+      }
+      const TileMaps* per_sweep[4] = {&sm.f1, &sm.f2, &sm.b, &sm.c};
+      for (int w = 0; w < 4; ++w) maps[static_cast<size_t>(w * 3 + t) * ctx->group_cap + k] = *per_sweep[w];
+    }
+  }
+  // Parameter packs (host; passed by value at every launch).
+  const int G = static_cast<int>(members.size());
+  ctx->group_size = G;
+  ctx->npacks = (G + kPackShots - 1) / kPackShots;
+  ctx->pack_nx.assign(ctx->npacks, 0);
+  for (int k = 0; k < G; ++k) ctx->pack_nx[k / kPackShots] = std::max(ctx->pack_nx[k / kPackShots], slots[k].g.nx);
+  if (G == 1) {
+    ctx->pack1.assign(12, SweepPack<1>{});
+    for (int w = 0; w < 12; ++w) {
+      ctx->pack1[w].maps[0] = maps[static_cast<size_t>(w) * ctx->group_cap];
+      ctx->pack1[w].slots[0] = slots[0];
+    }
+  } else {
+    ctx->packs.assign(static_cast<size_t>(12) * ctx->npacks, SweepPack<kPackShots>{});
+    for (int w = 0; w < 12; ++w)
+      for (int k = 0; k < G; ++k) {
+        SweepPack<kPackShots>& pk = ctx->packs[static_cast<size_t>(w) * ctx->npacks + k / kPackShots];
+        pk.maps[k % kPackShots] = maps[static_cast<size_t>(w) * ctx->group_cap + k];
+        pk.slots[k % kPackShots] = slots[k];
+      }
+  }
+  // Device copy of the slots for the gradient reduction.
+  CK(cudaMemcpyAsync(ctx->g_slots.p, slots.data(), slots.size() * sizeof(ShotSlot), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return FWIGB_OK;
+}
+
+// Tile-width autotuner: times every width of each sweep on the first group of
+// the first run (a few launches each on its live buffers, which the run then
+// resets) and keeps the fastest. The backward sweeps are tuned on the first
+// run with the adjoint.
+int autotune(fwigb_ctx* ctx, int nshots, int nx_max, bool adj) {
+  cudaStream_t s = ctx->stream;
   unsigned* d_err = reinterpret_cast<unsigned*>(ctx->scal.as<char>() + 16);
+  (void)nx_max;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  const int kinds_end = (adj && ctx->p.nSteps >= 2) ? 4 : 2;
+  const int kinds_end = (adj && ctx->nSteps_max >= 2) ? 4 : 2;
   for (int kind = ctx->tuned_fwd ? 2 : 0; kind < kinds_end; ++kind) {
     float best = 1e30f;
     for (int slot = 0; slot < 3; ++slot) {
       const int tx = kTileXs[slot];
-      const SweepMaps& mp = ctx->maps[slot];
-      auto launch = [&]() {
-        switch (kind) {
-          case 0: launch_fwd_stress(s, tx, mp.f1, g, f, m, c, sh, st, 0, false, d_err); break;
-          case 1: launch_fwd_velocity(s, tx, mp.f2, g, f, m, c, d_err); break;
-          case 2: launch_bwd_B(s, tx, mp.b, g, f, m, c, sh, st, gr, 0, d_err); break;
-          default: launch_bwd_C(s, tx, mp.c, g, f, m, c, sh, st, gr, 1, true, d_err); break;
-        }
-      };
+      auto launch = [&]() { launch_sweep(ctx, kind, tx, nshots, 0, false, d_err); };
       for (int w = 0; w < 2; ++w) launch();
       CK(cudaEventRecord(e0, s));
       for (int r = 0; r < 10; ++r) launch();
@@ -745,7 +960,7 @@ int run(fwigb_ctx* ctx, int calc_id) {
     ctx->err = "no model set";
     return FWIGB_ERR_ARG;
   }
-  if (ctx->staged.empty()) {
+  if (ctx->plans.empty()) {
     ctx->err = "no shots staged";
     return FWIGB_ERR_ARG;
   }
@@ -755,49 +970,14 @@ int run(fwigb_ctx* ctx, int calc_id) {
     return FWIGB_ERR_ARG;
   }
   CK(cudaSetDevice(ctx->device));
-  const Params& p = ctx->p;
-  const Geo& g = ctx->geo;
-  const int nt = p.nSteps, nrm = ctx->nrec_max;
-  const size_t ns = ctx->staged.size();
-  const size_t per = static_cast<size_t>(nrm) * nt;
+  std::vector<std::vector<int>> groups;
+  TRY_RC(plan_groups(ctx, adj, groups));
   cudaStream_t s = ctx->stream;
-  if (adj) {
-    const size_t store_bytes = static_cast<size_t>(nt) * 5 * g.ring_len * sizeof(float);
-    CK(ctx->store.ensure(store_bytes));
-  }
-  if (ctx->autotune && (!ctx->tuned_fwd || (adj && !ctx->tuned_bwd))) {
-    const StagedShot& S0 = ctx->staged[0];
-    ShotD sh{};
-    sh.src_z = S0.geom->z_src;
-    sh.src_x = S0.geom->x_src;
-    sh.src_szz = ctx->shot_src.as<float>(0);
-    sh.src_sxx = ctx->shot_src.as<float>(nt);
-    sh.nrec = S0.nrec;
-    sh.nSteps = nt;
-    sh.rec_z = ctx->shot_rec.as<int>(0);
-    sh.rec_x = sh.rec_z + nrm;
-    sh.blk_off = ctx->shot_blk.as<int>(0);
-    sh.blk_rec = sh.blk_off + ctx->nblk + 1;
-    sh.nbin_z = ctx->nbin_z;
-    sh.data = ctx->shot_data.as<float>(ns * per);
-    sh.res = ctx->shot_data.as<float>(2 * ns * per);
-    sh.gstf = ctx->shot_gstf.as<float>(0);
-    TRY_RC(autotune(ctx, sh, adj));
-  }
-  if (adj) {
-    CK(cudaMemsetAsync(ctx->grads.p, 0, 3 * ctx->cells * sizeof(float), s));
-    CK(cudaMemsetAsync(ctx->shot_gstf.p, 0, ns * nt * sizeof(float), s));
-  }
+  const int nz = ctx->p.nz;
+  unsigned* d_err = reinterpret_cast<unsigned*>(ctx->scal.as<char>() + 16);
   double* d_misfit = ctx->scal.as<double>();
   CK(cudaMemsetAsync(d_misfit, 0, sizeof(double), s));
-  Fields f = fields_of(ctx);
-  MediaD m = media_of(ctx);
-  CpmlD c = cpml_of(ctx);
-  StoreD st{ctx->store.as<float>()};
-  float* gb = ctx->grads.as<float>();
-  Grads gr{gb, gb + ctx->cells, gb + 2 * ctx->cells};
-  unsigned* d_err = reinterpret_cast<unsigned*>(ctx->scal.as<char>() + 16);
-  auto mp = [&](int kind) -> const SweepMaps& { return ctx->maps[tx_slot(ctx->tx[kind])]; };
+  if (adj) CK(cudaMemsetAsync(ctx->grads.p, 0, 3 * ctx->cells * sizeof(float), s));
   long long launches = 0;
   ctx->ev_kind.clear();
   size_t ev_used = 0;
@@ -821,63 +1001,81 @@ int run(fwigb_ctx* ctx, int calc_id) {
       launch;                                                            \
     }                                                                    \
   } while (0)
-  for (size_t is = 0; is < ns; ++is) {
-    const StagedShot& S = ctx->staged[is];
-    ShotD sh{};
-    sh.src_z = S.geom->z_src;
-    sh.src_x = S.geom->x_src;
-    sh.src_szz = ctx->shot_src.as<float>((2 * is) * nt);
-    sh.src_sxx = ctx->shot_src.as<float>((2 * is + 1) * nt);
-    sh.nrec = S.nrec;
-    sh.nSteps = nt;
-    sh.rec_z = ctx->shot_rec.as<int>(2 * is * nrm);
-    sh.rec_x = sh.rec_z + nrm;
-    sh.blk_off = ctx->shot_blk.as<int>(is * (ctx->nblk + 1 + nrm));
-    sh.blk_rec = sh.blk_off + ctx->nblk + 1;
-    sh.nbin_z = ctx->nbin_z;
-    float* d_obs = ctx->shot_data.as<float>(is * per);
-    float* d_syn = ctx->shot_data.as<float>((ns + is) * per);
-    float* d_res = ctx->shot_data.as<float>((2 * ns + is) * per);
-    sh.data = d_syn;
-    sh.res = d_res;
-    sh.gstf = ctx->shot_gstf.as<float>(is * nt);
-    // Fresh wavefields for each shot (libCUFD.cu:163-182) and an empty gather.
-    CK(cudaMemsetAsync(ctx->fields.p, 0, 18 * ctx->cells * sizeof(float), s));
-    CK(cudaMemsetAsync(d_syn, 0, per * sizeof(float), s));
-    for (int it = 0; it <= nt - 2; ++it) {
-      TIMED(0, launch_fwd_stress(s, ctx->tx[0], mp(0).f1, g, f, m, c, sh, st, it, adj, d_err));
-      TIMED(1, launch_fwd_velocity(s, ctx->tx[1], mp(1).f2, g, f, m, c, d_err));
-      launches += 2;
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    const std::vector<int>& mem = groups[gi];
+    const int G = static_cast<int>(mem.size());
+    int nx_max = 0;
+    TRY_RC(build_group(ctx, mem, nx_max));
+    if (ctx->autotune && (!ctx->tuned_fwd || (adj && !ctx->tuned_bwd))) TRY_RC(autotune(ctx, G, nx_max, adj));
+    const ShotSlot* slots = ctx->g_slots.as<ShotSlot>();
+    (void)nx_max;
+    std::vector<int> nst(G);
+    for (int k = 0; k < G; ++k) nst[k] = ctx->plans[mem[k]].nSteps;  // descending
+    auto active = [&](int step) {  // members whose record reaches `step`
+      int a = G;
+      while (a > 0 && nst[a - 1] - 2 < step) --a;
+      return a;
+    };
+    // Fresh wavefields and gathers for every member (libCUFD.cu:163-187).
+    CK(cudaMemsetAsync(ctx->g_fields.p, 0, static_cast<size_t>(G) * ctx->fields_stride * sizeof(float), s));
+    for (int k = 0; k < G; ++k) {
+      const ShotPlan& pl = ctx->plans[mem[k]];
+      const size_t per = static_cast<size_t>(pl.nrec) * pl.nSteps;
+      CK(cudaMemsetAsync(ctx->shot_data.as<float>(pl.data_off + per), 0, per * sizeof(float), s));
+      if (adj) CK(cudaMemsetAsync(ctx->shot_gstf.as<float>(pl.gstf_off), 0, pl.nSteps * sizeof(float), s));
+    }
+    if (adj) CK(cudaMemsetAsync(ctx->g_grads.p, 0, static_cast<size_t>(G) * ctx->grads_stride * sizeof(float), s));
+    const int ntop = nst[0];
+    for (int it = 0; it <= ntop - 2; ++it) {
+      const int a = active(it);
+      TIMED(0, launches += launch_sweep(ctx, 0, ctx->tx[0], a, it, adj, d_err));
+      TIMED(1, launches += launch_sweep(ctx, 1, ctx->tx[1], a, 0, false, d_err));
     }
     if (if_res) {
-      const float* tw = ctx->shot_taper.as<float>();
-      const float* to = ctx->per_trace_taper ? tw + (2 * is) * per : tw;
-      const float* tr = ctx->per_trace_taper ? tw + (2 * is + 1) * per : tw + nt;
-      const int nb = residual_blocks(S.nrec * nt);
-      launch_residual(s, S.nrec, nt, d_obs, d_syn, d_res, to, tr, ctx->per_trace_taper ? 1 : 0,
-                      ctx->partials.as<double>());
-      launch_sum_partials(s, ctx->partials.as<double>(), nb, d_misfit);
-      launches += 2;
-    }
-    if (adj) {
-      // Zero the adjoint fields and the 8 memory arrays (libCUFD.cu:337-351).
-      CK(cudaMemsetAsync(f.vz_a, 0, 13 * ctx->cells * sizeof(float), s));
-      // The reference's first el_velocity_adj acts on all-zero fields (no-op);
-      // then res_injection(nSteps-1) + el_stress_adj, source_grad(nSteps-2),
-      // reverse velocity of step nSteps-2 ... (libCUFD.cu:353-445).
-      TIMED(3, launch_bwd_C(s, ctx->tx[3], mp(3).c, g, f, m, c, sh, st, gr, nt - 1, nt - 1 >= 1, d_err));
-      ++launches;
-      for (int it = nt - 2; it >= 0; --it) {
-        TIMED(2, launch_bwd_B(s, ctx->tx[2], mp(2).b, g, f, m, c, sh, st, gr, it, d_err));
-        TIMED(3, launch_bwd_C(s, ctx->tx[3], mp(3).c, g, f, m, c, sh, st, gr, it, it >= 1, d_err));
+      for (int k = 0; k < G; ++k) {
+        const ShotPlan& pl = ctx->plans[mem[k]];
+        const int nt = pl.nSteps;
+        const size_t per = static_cast<size_t>(pl.nrec) * nt;
+        const float* tw = ctx->shot_taper.as<float>(pl.taper_off);
+        const float* to = tw;
+        const float* tr = ctx->per_trace_taper ? tw + per : tw + nt;
+        const int nb = residual_blocks(pl.nrec * nt);
+        launch_residual(s, pl.nrec, nt, ctx->shot_data.as<float>(pl.data_off),
+                        ctx->shot_data.as<float>(pl.data_off + per), ctx->shot_data.as<float>(pl.data_off + 2 * per),
+                        to, tr, ctx->per_trace_taper ? 1 : 0, ctx->partials.as<double>());
+        launch_sum_partials(s, ctx->partials.as<double>(), nb, d_misfit);
         launches += 2;
       }
     }
+    if (adj) {
+      // Zero the adjoint fields and the 8 memory arrays (libCUFD.cu:337-351):
+      // field slots 5..17 of every member.
+      for (int k = 0; k < G; ++k) {
+        const size_t n = static_cast<size_t>(ctx->geo.ldz) * ctx->plans[mem[k]].nx;
+        CK(cudaMemsetAsync(ctx->g_fields.as<float>(k * ctx->fields_stride + 5 * n), 0, 13 * n * sizeof(float), s));
+      }
+      // The reference's first el_velocity_adj acts on all-zero fields (no-op);
+      // then res_injection(nSteps-1) + el_stress_adj, source_grad(nSteps-2),
+      // reverse velocity of step nSteps-2 ... (libCUFD.cu:353-445), with
+      // backward iteration j meaning step nSteps_k - 2 - j of member k.
+      TIMED(3, launches += launch_sweep(ctx, 3, ctx->tx[3], G, -1, false, d_err));
+      for (int j = 0; j <= ntop - 2; ++j) {
+        const int a = active(j);
+        TIMED(2, launches += launch_sweep(ctx, 2, ctx->tx[2], a, j, false, d_err));
+        TIMED(3, launches += launch_sweep(ctx, 3, ctx->tx[3], a, j, false, d_err));
+      }
+      float* gb = ctx->grads.as<float>();
+      launch_reduce_grads(s, nz, ctx->p.nx, ctx->geo.ldz, G, slots, gb, gb + ctx->cells, gb + 2 * ctx->cells);
+      ++launches;
+    }
+    // The next group reuses the slots and maps; wait for this one.
+    if (gi + 1 < groups.size()) CK(cudaStreamSynchronize(s));
   }
 #undef TIMED
   CK(cudaGetLastError());
   ctx->launches = launches;
   ctx->last_calc = calc_id;
+  ctx->last_groups = static_cast<int>(groups.size());
   return FWIGB_OK;
 }
 
@@ -902,9 +1100,7 @@ int fetch(fwigb_ctx* ctx, double* misfit, double* g_lam, double* g_mu, double* g
   cudaStream_t s = ctx->stream;
   const Params& p = ctx->p;
   const size_t n = ctx->cells;
-  const size_t ns = ctx->staged.size();
-  const int nt = p.nSteps;
-  const size_t per = static_cast<size_t>(ctx->nrec_max) * nt;
+  const int nt_max = p.nSteps;
   {
     unsigned e = 0;
     CK(cudaMemcpyAsync(&e, ctx->scal.as<char>() + 16, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
@@ -936,34 +1132,53 @@ int fetch(fwigb_ctx* ctx, double* misfit, double* g_lam, double* g_mu, double* g
     }
   }
   if (g_stf) {
-    std::vector<float> h(ns * nt);
-    CK(cudaMemcpyAsync(h.data(), ctx->shot_gstf.p, h.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
+    // Row k: shot k's source gradient, zero past its record length.
+    size_t tot = 0;
+    for (const ShotPlan& pl : ctx->plans) tot += pl.nSteps;
+    std::vector<float> h(tot);
+    CK(cudaMemcpyAsync(h.data(), ctx->shot_gstf.p, tot * sizeof(float), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    for (size_t k = 0; k < h.size(); ++k) g_stf[k] = h[k];
+    for (size_t k = 0; k < ctx->plans.size(); ++k) {
+      const ShotPlan& pl = ctx->plans[k];
+      for (int it = 0; it < nt_max; ++it)
+        g_stf[k * nt_max + it] = it < pl.nSteps ? static_cast<double>(h[pl.gstf_off + it]) : 0.0;
+    }
   }
   if (gathers) {
-    CK(cudaMemcpyAsync(gathers, ctx->shot_data.as<float>(ns * per), ns * per * sizeof(float),
-                       cudaMemcpyDeviceToHost, s));
+    // Shot k at offset k * nrec_max * nSteps as [nrec][nSteps], its
+    // [nrec_k][nSteps_k] block in the top-left corner.
+    const size_t blk = static_cast<size_t>(ctx->nrec_max) * nt_max;
+    std::memset(gathers, 0, ctx->plans.size() * blk * sizeof(float));
+    for (size_t k = 0; k < ctx->plans.size(); ++k) {
+      const ShotPlan& pl = ctx->plans[k];
+      const size_t per = static_cast<size_t>(pl.nrec) * pl.nSteps;
+      CK(cudaMemcpy2DAsync(gathers + k * blk, nt_max * sizeof(float), ctx->shot_data.as<float>(pl.data_off + per),
+                           pl.nSteps * sizeof(float), pl.nSteps * sizeof(float), pl.nrec, cudaMemcpyDeviceToHost, s));
+    }
   }
   CK(cudaStreamSynchronize(s));
   return FWIGB_OK;
 }
 
 int write_gathers(fwigb_ctx* ctx, const float* gathers) {
-  // libCUFD.cu:514-521.
-  const int nt = ctx->p.nSteps;
-  const size_t per = static_cast<size_t>(ctx->nrec_max) * nt;
-  for (size_t s = 0; s < ctx->staged.size(); ++s) {
-    const std::string fn = ctx->p.data_dir_name + "/Shot" + std::to_string(ctx->staged[s].id) + ".bin";
+  // libCUFD.cu:514-521, [nrec][nSteps_k] float per shot.
+  const int nt_max = ctx->p.nSteps;
+  const size_t blk = static_cast<size_t>(ctx->nrec_max) * nt_max;
+  std::vector<float> row;
+  for (size_t k = 0; k < ctx->plans.size(); ++k) {
+    const ShotPlan& pl = ctx->plans[k];
+    const std::string fn = ctx->p.data_dir_name + "/Shot" + std::to_string(pl.id) + ".bin";
     std::FILE* fp = std::fopen(fn.c_str(), "wb");
     if (!fp) {
       ctx->err = "cannot write " + fn;
       return FWIGB_ERR_IO;
     }
-    const size_t want = static_cast<size_t>(ctx->staged[s].nrec) * nt;
-    const size_t put = std::fwrite(gathers + s * per, sizeof(float), want, fp);
+    bool ok = true;
+    for (int r = 0; r < pl.nrec && ok; ++r)
+      ok = std::fwrite(gathers + k * blk + static_cast<size_t>(r) * nt_max, sizeof(float), pl.nSteps, fp) ==
+           static_cast<size_t>(pl.nSteps);
     std::fclose(fp);
-    if (put != want) {
+    if (!ok) {
       ctx->err = "short write to " + fn;
       return FWIGB_ERR_IO;
     }
@@ -971,16 +1186,14 @@ int write_gathers(fwigb_ctx* ctx, const float* gathers) {
   return FWIGB_OK;
 }
 
-#define TRY(call)            \
-  do {                       \
-    int rc_ = (call);        \
+#define TRY(call)                    \
+  do {                               \
+    int rc_ = (call);                \
     if (rc_ != FWIGB_OK) return rc_; \
   } while (0)
 
 }  // namespace
 
-// ---------------------------------------------------------------------------
-// C ABI
 extern "C" {
 
 int fwigb_create(const char* para_fname, int device, fwigb_ctx** out) {
@@ -1008,9 +1221,10 @@ int fwigb_destroy(fwigb_ctx* ctx) {
   if (!ctx) return FWIGB_OK;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  for (DevBuf* b : {&ctx->media, &ctx->stage, &ctx->cpml, &ctx->fields, &ctx->grads, &ctx->store, &ctx->scal,
-                    &ctx->partials, &ctx->shot_src, &ctx->shot_rec, &ctx->shot_blk, &ctx->shot_data,
-                    &ctx->shot_taper, &ctx->shot_gstf})
+  for (DevBuf* b : {&ctx->media, &ctx->stage, &ctx->cpml, &ctx->grads, &ctx->scal, &ctx->partials,
+                    &ctx->shot_src, &ctx->shot_rec, &ctx->shot_blk, &ctx->shot_data, &ctx->shot_taper,
+                    &ctx->shot_gstf, &ctx->shot_cpmlx, &ctx->g_fields, &ctx->g_store, &ctx->g_grads,
+                    &ctx->g_slots})
     b->release();
   for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1037,6 +1251,17 @@ int fwigb_shot_nrec(const fwigb_ctx* ctx, int shot_id, int* nrec) {
       !ctx->survey[shot_id].present)
     return FWIGB_ERR_ARG;
   *nrec = static_cast<int>(ctx->survey[shot_id].z_rec.size());
+  return FWIGB_OK;
+}
+
+int fwigb_shot_info(const fwigb_ctx* ctx, int shot_id, int* nrec, int* nSteps, int* x_off, int* nx) {
+  if (!ctx || shot_id < 0 || shot_id >= static_cast<int>(ctx->survey.size()) || !ctx->survey[shot_id].present)
+    return FWIGB_ERR_ARG;
+  const ShotGeom& g = ctx->survey[shot_id];
+  if (nrec) *nrec = static_cast<int>(g.z_rec.size());
+  if (nSteps) *nSteps = g.nSteps;
+  if (x_off) *x_off = g.x_off;
+  if (nx) *nx = g.nx;
   return FWIGB_OK;
 }
 
@@ -1100,6 +1325,16 @@ int fwigb_set_tile_config(fwigb_ctx* ctx, const int* tile_x) {
   return FWIGB_OK;
 }
 
+int fwigb_set_batching(fwigb_ctx* ctx, int max_shots, unsigned long long mem_budget_bytes) {
+  if (!ctx || max_shots < 0) return FWIGB_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->max_batch = max_shots;
+  ctx->mem_budget = static_cast<size_t>(mem_budget_bytes);
+  return FWIGB_OK;
+}
+
+int fwigb_last_group_count(const fwigb_ctx* ctx) { return ctx ? ctx->last_groups : -1; }
+
 int fwigb_set_kernel_timing(fwigb_ctx* ctx, int enable) {
   if (!ctx) return FWIGB_ERR_ARG;
   std::lock_guard<std::mutex> lk(ctx->mu);
@@ -1156,7 +1391,7 @@ int fwigb_obs(fwigb_ctx* ctx, const double* lambda, const double* mu, const doub
   std::vector<float> tmp;
   float* out = gathers;
   if (!out && write_files) {
-    tmp.resize(ctx->staged.size() * static_cast<size_t>(ctx->nrec_max) * ctx->p.nSteps);
+    tmp.resize(ctx->plans.size() * static_cast<size_t>(ctx->nrec_max) * ctx->p.nSteps);
     out = tmp.data();
   }
   if (out) TRY(fetch(ctx, nullptr, nullptr, nullptr, nullptr, nullptr, out));

@@ -96,27 +96,65 @@ struct Grads {
   float* den;
 };
 
+// Everything one shot's sweeps need, for a shot running on its own sub-grid
+// (an aperture window of the model: padded columns x_off .. x_off + g.nx - 1)
+// with its own record length. Media pointers are views of the global media
+// shifted by x_off columns; CPML x profiles are those of the sub-grid width.
+struct ShotSlot {
+  Geo g;
+  Fields f;
+  MediaD m;
+  CpmlD c;
+  ShotD sh;
+  StoreD st;
+  Grads gr;  // this shot's gradient on its sub-grid
+  int nSteps;
+  int x_off;
+};
+
 // Tensor maps of the sweeps for one tile width: F1 stages vz, vx; F2 szz,
 // sxx, sxz; B vz, vx, szz_a, sxx_a, sxz_a; C vz_a, vx_a, szz, sxx, sxz.
 struct SweepMaps {
   TileMaps f1, f2, b, c;
 };
 
+// What one sweep launch reads for up to K shots, passed by value as a
+// __grid_constant__ kernel parameter: the block of shot k reads its slot and
+// tensor maps from the constant bank (no global-memory round trip before its
+// first stencil load). K = 1 for a lone shot; kPackShots for a batch, which
+// keeps the parameter block under the 32 KB kernel-parameter limit.
+constexpr int kPackShots = 16;
+template <int K>
+struct alignas(64) SweepPack {
+  TileMaps maps[K];
+  ShotSlot slots[K];
+};
+static_assert(sizeof(SweepPack<kPackShots>) < 32000, "sweep pack exceeds the kernel parameter limit");
+
 // Encodes the sweep tensor maps for tile width tx (host; needs the driver's
 // cuTensorMapEncodeTiled). Returns false with a message on failure.
 bool encode_sweep_maps(const Geo& g, const Fields& f, int tx, SweepMaps& out, const char** err);
 
-// ---- launchers (kernels.cu). tx selects the tile width; err is a device
+// ---- launchers (kernels.cu). One launch covers the first `nshots` (<= K)
+// shots of a pack. nx_max is the widest sub-grid among them. err is a device
 // word that a sweep sets when a bounded wait for its staged tiles gives up.
-void launch_fwd_stress(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
-                       const CpmlD& c, const ShotD& sh, const StoreD& st, int it, bool save, unsigned* err);
-void launch_fwd_velocity(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
-                         const CpmlD& c, unsigned* err);
-void launch_bwd_B(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
-                  const CpmlD& c, const ShotD& sh, const StoreD& st, const Grads& gr, int it, unsigned* err);
-void launch_bwd_C(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
-                  const CpmlD& c, const ShotD& sh, const StoreD& st, const Grads& gr, int it, bool rev,
+// The backward sweeps take the backward iteration j; shot k works on its step
+// nSteps_k - 2 - j. Instantiated for K = 1 and K = kPackShots.
+template <int K>
+void launch_fwd_stress(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max, int it,
+                       bool save, unsigned* err);
+template <int K>
+void launch_fwd_velocity(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max,
+                         unsigned* err);
+template <int K>
+void launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max, int j,
                   unsigned* err);
+template <int K>
+void launch_bwd_C(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max, int j,
+                  unsigned* err);
+// Adds the per-shot gradients of the first nshots slots into the global ones.
+void launch_reduce_grads(cudaStream_t s, int nz, int nx, int ldz, int nshots, const ShotSlot* slots, float* g_lam,
+                         float* g_mu, float* g_den);
 
 // Model set-up: row-major double (lambda, mu in MPa) -> column-major float media.
 // cpmax_bits receives atomicMax of the P velocity's float bits.

@@ -69,9 +69,10 @@ __device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* tm, i
 
 // Starts staging NA arrays of the tile at (z0, x0) into shared memory: one
 // 2-D TMA copy each of the box [z0-4, z0+36) x [x0-2, x0+TX+2), zero filled
-// outside the grid. Thread (0,0) initialises the mbarrier and issues the
-// copies; the caller then loads its own-cell operands (which overlap with the
-// copies) and calls stage_wait.
+// outside the grid. The leader initialises the mbarrier (fenced so the copies
+// see it) and issues the copies after the block has met the barrier's
+// initialisation; the caller then loads its own-cell operands (which overlap
+// with the copies) and calls stage_wait.
 template <int NA, int TX>
 __device__ __forceinline__ void stage_begin(const TileMaps& mp, float* sm, uint64_t* bar, int z0, int x0) {
   constexpr int N = kBoxZ * (TX + 4);
@@ -138,22 +139,36 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
   return make_int2(sh.blk_off[b], sh.blk_off[b + 1]);
 }
 
-// Thread layout of every sweep: block (32, TX), one cell per thread; lane
-// threadIdx.x is the depth offset, threadIdx.y the column offset in the tile.
-// `b` is the cell's index in a staged box (column stride kBoxZ).
+// Every sweep is launched once per time step for a group of shots: blockIdx.z
+// is the shot (its slot holds its sub-grid, fields, source, receivers and
+// TMA maps), blockIdx.x / blockIdx.y the tile of 32 depths x TX columns. The
+// launch covers the group's widest shot; blocks past a narrower shot's grid
+// leave before staging anything. Block (32, TX), one cell per thread: lane
+// threadIdx.x is the depth offset, threadIdx.y the column offset; `b` is the
+// cell's index in a staged box (column stride kBoxZ).
 #define SWEEP_SETUP(NA)                                                        \
   constexpr int N = kBoxZ * (TX + 4);                                          \
   extern __shared__ __align__(128) float sm[];                                 \
   __shared__ __align__(8) uint64_t bar;                                        \
+  const int shot = K == 1 ? 0 : static_cast<int>(blockIdx.z);                  \
+  const ShotSlot& S = P.slots[shot];                                           \
+  const Geo& g = S.g;                                                          \
   const int z0 = blockIdx.x * kTileZ, x0 = blockIdx.y * TX;                    \
-  stage_begin<NA, TX>(mp, sm, &bar, z0, x0);                                   \
+  if (z0 >= g.nz || x0 >= g.nx) return; /* block-uniform */                    \
+  stage_begin<NA, TX>(P.maps[shot], sm, &bar, z0, x0);                         \
+  const Fields& f = S.f;                                                       \
+  const MediaD& m = S.m;                                                       \
+  const CpmlD& c = S.c;                                                        \
   const int z = z0 + threadIdx.x, x = x0 + threadIdx.y;                        \
   if (z >= g.nz || x >= g.nx) return;                                          \
   const size_t ldz = static_cast<size_t>(g.ldz);                               \
   const size_t i = static_cast<size_t>(x) * ldz + z;                           \
   const int b = (threadIdx.y + 2) * kBoxZ + threadIdx.x + 4;                   \
   (void)N;                                                                     \
-  (void)b;
+  (void)b;                                                                     \
+  (void)f;                                                                     \
+  (void)m;                                                                     \
+  (void)c;
 
 // Register budgets: forward sweeps 64 registers (32 warps per SM), backward
 // sweeps 80 (24 warps per SM).
@@ -164,10 +179,11 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
 // F1: el_stress (el_stress.cu:50-88) + add_source (utilities.cu:521-541) +
 // recording (utilities.cu:557-567) + from_bnd of the 5 fields (Boundary.cu:55-76).
 // Staged: vz, vx.
-template <int TX>
-__global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c,
-                                        ShotD sh, StoreD st, int it, int save, unsigned* err) {
+template <int TX, int K>
+__global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ SweepPack<K> P, int it, int save, unsigned* err) {
   SWEEP_SETUP(2)
+  const ShotD& sh = S.sh;
+  const StoreD& st = S.st;
   float szz = f.szz[i], sxx = f.sxx[i], sxz = f.sxz[i];
   const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
   if (!stage_wait(&bar, err)) return;
@@ -229,9 +245,8 @@ __global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ TileMaps mp, Geo
 }
 
 // F2: el_velocity, isFor = true (el_velocity.cu:45-82). Staged: szz, sxx, sxz.
-template <int TX>
-__global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c,
-                                          unsigned* err) {
+template <int TX, int K>
+__global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ SweepPack<K> P, unsigned* err) {
   SWEEP_SETUP(3)
   const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
   float vz = 0.0f, vx = 0.0f, bA = 0.0f, bB = 0.0f;
@@ -272,10 +287,13 @@ __global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ TileMaps mp, G
 // ---------------------------------------------------------------------------
 // B: add_source(-) + el_stress(isFor=false) with the lambda / mu kernels +
 // to_bnd(stress) + el_velocity_adj. Staged: vz, vx, szz_a, sxx_a, sxz_a.
-template <int TX>
-__global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c, ShotD sh,
-                                   StoreD st, Grads gr, int it, unsigned* err) {
+template <int TX, int K>
+__global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
   SWEEP_SETUP(5)
+  const ShotD& sh = S.sh;
+  const StoreD& st = S.st;
+  const Grads& gr = S.gr;
+  const int it = S.nSteps - 2 - j;  // this shot's time step at backward iteration j
   const float dt = g.dt;
   float szz = f.szz[i], sxx = f.sxx[i], sxz = f.sxz[i];
   const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
@@ -386,10 +404,17 @@ __global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ TileMaps mp, Geo g, F
 //    + source_grad (utilities.cu:582-593) + el_velocity(isFor=false) with the
 //    density kernel (el_velocity.cu:220-244) + to_bnd(velocity).
 //    Staged: vz_a, vx_a, szz, sxx, sxz.
-template <int TX>
-__global__ void BWD_BOUNDS k_bwd_C(const __grid_constant__ TileMaps mp, Geo g, Fields f, MediaD m, CpmlD c, ShotD sh,
-                                   StoreD st, Grads gr, int it, int rev, unsigned* err) {
+template <int TX, int K>
+__global__ void BWD_BOUNDS k_bwd_C(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
   SWEEP_SETUP(5)
+  const ShotD& sh = S.sh;
+  const StoreD& st = S.st;
+  const Grads& gr = S.gr;
+  // Backward iteration j handles res_injection + el_stress_adj of step
+  // it = nSteps - 2 - j (j = -1: the shot's last step) and the reverse
+  // velocity of step it - 1.
+  const int it = S.nSteps - 2 - j;
+  const int rev = it >= 1;
   const float dt = g.dt;
   float sa = f.szz_a[i], xa = f.sxx_a[i], za = f.sxz_a[i];
   const float bA = m.bycA[i], bB = m.bycB[i], amu = m.aveMu[i], lam = m.lam[i], l2m = m.l2m[i];
@@ -616,6 +641,29 @@ __global__ void __launch_bounds__(kResThreads)
   }
 }
 
+// Adds the per-shot gradients of a shot group into the global gradients, in
+// group order (deterministic): shot k's sub-grid column j is global padded
+// column x_off[k] + j.
+__global__ void k_reduce_grads(int nz, int nx, int ldz, int nshots, const ShotSlot* __restrict__ slots, float* g_lam,
+                               float* g_mu, float* g_den) {
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  const int x = blockIdx.y * blockDim.y + threadIdx.y;
+  if (z >= nz || x >= nx) return;
+  const size_t i = static_cast<size_t>(x) * ldz + z;
+  float a = g_lam[i], b = g_mu[i], c = g_den[i];
+  for (int k = 0; k < nshots; ++k) {
+    const int xs = x - slots[k].x_off;
+    if (xs < 0 || xs >= slots[k].g.nx) continue;
+    const size_t j = static_cast<size_t>(xs) * ldz + z;
+    a += slots[k].gr.lam[j];
+    b += slots[k].gr.mu[j];
+    c += slots[k].gr.den[j];
+  }
+  g_lam[i] = a;
+  g_mu[i] = b;
+  g_den[i] = c;
+}
+
 // Fixed-order sum of the block partials into *acc (one warp).
 __global__ void k_sum_partials(const double* __restrict__ partials, int n, double* acc) {
   double v = 0.0;
@@ -630,8 +678,8 @@ __global__ void k_sum_partials(const double* __restrict__ partials, int n, doubl
 namespace {
 
 template <int TX>
-dim3 sweep_grid(const Geo& g) {
-  return dim3((g.nz + kTileZ - 1) / kTileZ, (g.nx + TX - 1) / TX);
+dim3 sweep_grid(int nz, int nx_max, int nshots) {
+  return dim3((nz + kTileZ - 1) / kTileZ, (nx_max + TX - 1) / TX, nshots);
 }
 template <int TX>
 constexpr size_t smem_bytes(int na) {
@@ -659,30 +707,42 @@ constexpr size_t smem_bytes(int na) {
     }                               \
   }
 
-void launch_fwd_stress(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
-                       const CpmlD& c, const ShotD& sh, const StoreD& st, int it, bool save, unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, (k_fwd_stress<TX><<<sweep_grid<TX>(g), dim3(32, TX), smem_bytes<TX>(2), s>>>(
-                            mp, g, f, m, c, sh, st, it, save ? 1 : 0, err)))
+template <int K>
+void launch_fwd_stress(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max, int it,
+                       bool save, unsigned* err) {
+  FWIGB_DISPATCH_TX(tx, (k_fwd_stress<TX, K><<<sweep_grid<TX>(nz, nx_max, nshots), dim3(32, TX), smem_bytes<TX>(2),
+                                              s>>>(p, it, save ? 1 : 0, err)))
 }
 
-void launch_fwd_velocity(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
-                         const CpmlD& c, unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, (k_fwd_velocity<TX><<<sweep_grid<TX>(g), dim3(32, TX), smem_bytes<TX>(3), s>>>(
-                            mp, g, f, m, c, err)))
+template <int K>
+void launch_fwd_velocity(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max,
+                         unsigned* err) {
+  FWIGB_DISPATCH_TX(tx, (k_fwd_velocity<TX, K><<<sweep_grid<TX>(nz, nx_max, nshots), dim3(32, TX),
+                                                smem_bytes<TX>(3), s>>>(p, err)))
 }
 
-void launch_bwd_B(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
-                  const CpmlD& c, const ShotD& sh, const StoreD& st, const Grads& gr, int it, unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, (k_bwd_B<TX><<<sweep_grid<TX>(g), dim3(32, TX), smem_bytes<TX>(5), s>>>(
-                            mp, g, f, m, c, sh, st, gr, it, err)))
-}
-
-void launch_bwd_C(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, const Fields& f, const MediaD& m,
-                  const CpmlD& c, const ShotD& sh, const StoreD& st, const Grads& gr, int it, bool rev,
+template <int K>
+void launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max, int j,
                   unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, (k_bwd_C<TX><<<sweep_grid<TX>(g), dim3(32, TX), smem_bytes<TX>(5), s>>>(
-                            mp, g, f, m, c, sh, st, gr, it, rev ? 1 : 0, err)))
+  FWIGB_DISPATCH_TX(tx, (k_bwd_B<TX, K><<<sweep_grid<TX>(nz, nx_max, nshots), dim3(32, TX), smem_bytes<TX>(5), s>>>(
+                            p, j, err)))
 }
+
+template <int K>
+void launch_bwd_C(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max, int j,
+                  unsigned* err) {
+  FWIGB_DISPATCH_TX(tx, (k_bwd_C<TX, K><<<sweep_grid<TX>(nz, nx_max, nshots), dim3(32, TX), smem_bytes<TX>(5), s>>>(
+                            p, j, err)))
+}
+
+#define FWIGB_INSTANTIATE(K)                                                                                      \
+  template void launch_fwd_stress<K>(cudaStream_t, int, const SweepPack<K>&, int, int, int, int, bool, unsigned*); \
+  template void launch_fwd_velocity<K>(cudaStream_t, int, const SweepPack<K>&, int, int, int, unsigned*);          \
+  template void launch_bwd_B<K>(cudaStream_t, int, const SweepPack<K>&, int, int, int, int, unsigned*);            \
+  template void launch_bwd_C<K>(cudaStream_t, int, const SweepPack<K>&, int, int, int, int, unsigned*);
+FWIGB_INSTANTIATE(1)
+FWIGB_INSTANTIATE(kPackShots)
+#undef FWIGB_INSTANTIATE
 
 // Tensor maps: one per staged array, a 2-D view (z inner, x outer; row stride
 // ldz floats) with the box kBoxZ x (TX + 4). cuTensorMapEncodeTiled checks
@@ -691,6 +751,7 @@ void launch_bwd_C(cudaStream_t s, int tx, const TileMaps& mp, const Geo& g, cons
 // 128); the x coordinate of every copy, z0 - 4 with z0 a multiple of 32, is a
 // multiple of 4 floats.
 bool encode_sweep_maps(const Geo& g, const Fields& f, int tx, SweepMaps& out, const char** err) {
+  // g is the shot's sub-grid; f its fields.
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
     void* fn = nullptr;
@@ -754,6 +815,12 @@ void launch_residual(cudaStream_t s, int nrec, int nSteps, const float* obs, flo
 
 void launch_sum_partials(cudaStream_t s, const double* partials, int n, double* acc) {
   k_sum_partials<<<1, 32, 0, s>>>(partials, n, acc);
+}
+
+void launch_reduce_grads(cudaStream_t s, int nz, int nx, int ldz, int nshots, const ShotSlot* slots, float* g_lam,
+                         float* g_mu, float* g_den) {
+  dim3 grid((nz + 31) / 32, (nx + 7) / 8);
+  k_reduce_grads<<<grid, dim3(32, 8), 0, s>>>(nz, nx, ldz, nshots, slots, g_lam, g_mu, g_den);
 }
 
 void launch_to_rowmajor(cudaStream_t s, int nz, int nx, int ldz, const float* src, double* dst, double scale) {

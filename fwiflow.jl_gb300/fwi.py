@@ -67,6 +67,13 @@ class FwiContext:
         _lib.check(self._lib.fwigb_shot_nrec(self._h, int(shot_id), _lib.ctypes.byref(v)), self._h)
         return v.value
 
+    def shot_info(self, shot_id: int):
+        """(nrec, nSteps, x_off, nx) of a survey shot: receivers, record length
+        and the padded columns of its sub-grid."""
+        vals = [_lib.ctypes.c_int() for _ in range(4)]
+        _lib.check(self._lib.fwigb_shot_info(self._h, int(shot_id), *(_lib.ctypes.byref(x) for x in vals)), self._h)
+        return tuple(x.value for x in vals)
+
     def _model(self, lam, mu, den):
         lam, mu, den = _f64(lam), _f64(mu), _f64(den)
         for a in (lam, mu, den):
@@ -85,8 +92,8 @@ class FwiContext:
         blk = np.zeros((len(ids), self.nrec_max, self.nSteps), dtype=np.float32)
         for i, (o, sid) in enumerate(zip(obs, ids)):
             o = np.asarray(o, dtype=np.float32)
-            nrec = self.nrec(sid)
-            blk[i, :nrec, :] = o.reshape(nrec, self.nSteps)
+            nrec, nt = self.shot_info(sid)[:2]
+            blk[i, :nrec, :nt] = o.reshape(nrec, nt)
         return blk
 
     # -- operator calls
@@ -133,7 +140,11 @@ class FwiContext:
         _lib.check(self._lib.fwigb_obs(self._h, _lib.dptr(lam), _lib.dptr(mu), _lib.dptr(den), _lib.dptr(stf),
                                        stf.shape[0], _lib.iptr(ids), len(ids), _lib.fptr(blk), int(write_files)),
                    self._h)
-        return [blk[i, :self.nrec(s), :] for i, s in enumerate(ids)]
+        out = []
+        for i, s in enumerate(ids):
+            nrec, nt = self.shot_info(s)[:2]
+            out.append(blk[i, :nrec, :nt])
+        return out
 
     # -- staged interface (model / shots resident on the device)
     def set_model(self, lam, mu, den) -> None:
@@ -169,6 +180,14 @@ class FwiContext:
 
     def last_launch_count(self) -> int:
         return int(self._lib.fwigb_last_launch_count(self._h))
+
+    def set_batching(self, max_shots: int = 0, mem_budget_bytes: int = 0) -> None:
+        """Cap the shots per concurrent group (0: none) and the group state's
+        device memory (0: 90% of free memory)."""
+        _lib.check(self._lib.fwigb_set_batching(self._h, int(max_shots), int(mem_budget_bytes)), self._h)
+
+    def last_group_count(self) -> int:
+        return int(self._lib.fwigb_last_group_count(self._h))
 
     def tile_config(self):
         """Tile widths of (forward stress, forward velocity, backward B, backward C)."""

@@ -125,6 +125,39 @@ def dipping_grf(seed: int = 2, nz: int = 512, nx: int = 1536, nSteps: int = 3000
     return Workload("dipping_grf", nz, nx, nPml, nPad, 10.0, 10.0, 0.001, nSteps, 10.0, vp, vp_obs, shots, stf)
 
 
+def batched_uneven(seed: int = 3, nz: int = 512, nx: int = 1536, n_shots: int = 64, width=(400, 1536),
+                   steps=(1500, 4000), f0=(8.0, 12.0), nSteps: Optional[int] = None) -> Workload:
+    """The dipping_grf model family with n_shots shots, each with its own
+    aperture window (width drawn uniformly in `width` interior columns,
+    centred on the source where the model allows), record length (uniform in
+    `steps`; the parameter file's nSteps is the largest) and Ricker frequency
+    (uniform in `f0`). Sources at depth 2 at seed-drawn columns; receivers on
+    every column of the window at depth 2."""
+    rng = np.random.default_rng(seed)
+    nPml = 32
+    nPad = default_nPad(nz, nPml)
+    base = _layers(nz, nx, 1500.0, 4500.0, 8, dip_deg=5.0)
+    pert = gaussian_random_field((nz, nx), 20.0, rng)
+    vp = padding(base * (1.0 + 0.03 * pert), nPml, nPad)
+    vp_obs = padding(base, nPml, nPad)
+    shots = []
+    nts, f0s = [], []
+    for _ in range(n_shots):
+        w = int(rng.integers(width[0], min(width[1], nx) + 1))
+        xs = int(rng.integers(4, nx - 4))
+        w0 = int(np.clip(xs - w // 2, 0, nx - w))
+        nt = int(rng.integers(steps[0], steps[1] + 1))
+        nts.append(nt)
+        f0s.append(float(rng.uniform(f0[0], f0[1])))
+        shots.append({"z_src": 2, "x_src": xs, "z_rec": [2] * w, "x_rec": list(range(w0, w0 + w)), "nSteps": nt,
+                      "win_x0": w0, "win_x1": w0 + w - 1})
+    nt_max = max(nts) if nSteps is None else nSteps
+    stf = np.concatenate([sourceGene(f, nt_max, 0.001) for f in f0s], axis=0)
+    w = Workload("batched_uneven", nz, nx, nPml, nPad, 10.0, 10.0, 0.001, nt_max, 10.0, vp, vp_obs, shots, stf)
+    w.extra["f0"] = f0s
+    return w
+
+
 def tiny(nz: int = 40, nx: int = 60, nPml: int = 12, nSteps: int = 300, n_shots: int = 2, seed: int = 0,
          cs_zero: bool = False) -> Workload:
     """Small smooth model with a Gaussian anomaly for parity tests (seconds on a CPU)."""

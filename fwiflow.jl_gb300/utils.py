@@ -97,7 +97,11 @@ def surveyGen_shots(shots: Sequence[dict], survey_fname: str) -> None:
 
     Each entry holds z_src, x_src, z_rec, x_rec (0-based interior indices) and
     optionally win_start, win_end, weights. The file format is the reference's
-    (`{"nShots": n, "shot0": {...}, ...}`, read by Src_Rec.cu:19-245).
+    (`{"nShots": n, "shot0": {...}, ...}`, read by Src_Rec.cu:19-245). Two
+    optional keys of this package, which the reference's parser ignores, are
+    passed through: "nSteps" (the shot's record length, at most the parameter
+    file's) and "win_x0" / "win_x1" (the shot's aperture window of interior
+    columns).
     """
     survey: dict = {"nShots": len(shots)}
     for i, s in enumerate(shots):
@@ -106,6 +110,9 @@ def surveyGen_shots(shots: Sequence[dict], survey_fname: str) -> None:
         for k in ("win_start", "win_end", "weights"):
             if k in s:
                 d[k] = [float(v) for v in s[k]]
+        for k in ("nSteps", "win_x0", "win_x1"):
+            if k in s:
+                d[k] = int(s[k])
         survey[f"shot{i}"] = d
     with open(survey_fname, "w") as f:
         f.write(json.dumps(survey, separators=(",", ":")))

@@ -97,6 +97,10 @@ int fwigb_geometry(const fwigb_ctx *ctx, int *nz, int *nx, int *nSteps, int *n_s
 /* Number of receivers of survey shot `shot_id`. */
 int fwigb_shot_nrec(const fwigb_ctx *ctx, int shot_id, int *nrec);
 
+/* Receivers, record length, first padded column and width of the sub-grid of
+ * survey shot `shot_id` (any pointer may be NULL). */
+int fwigb_shot_info(const fwigb_ctx *ctx, int shot_id, int *nrec, int *nSteps, int *x_off, int *nx);
+
 /* One-call drop-in for cufd itself (libCUFD.cu:34-38) with a C string for the
  * parameter file. calc_id 0 writes misfit, 1 writes the gradients (g_stf has
  * group_size rows), 2 writes Data/Shot<id>.bin. A context per (para_fname,
@@ -136,6 +140,18 @@ void *fwigb_stream(fwigb_ctx *ctx);
 
 /* Number of kernel launches the last fwigb_run issued (host-side count). */
 long long fwigb_last_launch_count(const fwigb_ctx *ctx);
+
+/* Concurrent shots. The shots of a call run in groups, all members of a group
+ * in the same launches (one per sweep and time step). A group holds at most
+ * max_shots shots (0: no cap) and its state (wavefields, gradients, boundary
+ * stores) at most mem_budget_bytes (0: 90% of the free device memory). Shots
+ * may carry their own record length ("nSteps") and aperture window
+ * ("win_x0", "win_x1", interior columns) as extra keys of the survey file;
+ * the reference's parser ignores those keys. */
+int fwigb_set_batching(fwigb_ctx *ctx, int max_shots, unsigned long long mem_budget_bytes);
+
+/* Number of shot groups the last fwigb_run used. */
+int fwigb_last_group_count(const fwigb_ctx *ctx);
 
 /* Tile widths (columns per thread block: 4, 8 or 16) of the four sweeps
  * (forward stress, forward velocity, backward B, backward C). By default an

@@ -7,6 +7,11 @@ bench.py (CPU baseline / reference arm). The product package never imports it.
   restating the reference's parameter and survey parsing (Parameter.cpp:16-178,
   Src_Rec.cu:19-245) and its file I/O of observed data (libCUFD.cu:189-192,
   514-521).
+* Shots of this package's survey extension (per-shot record length "nSteps"
+  and aperture window "win_x0" .. "win_x1" of interior columns) are defined
+  as the reference run alone on the shot's sub-model (padded columns win_x0 ..
+  win_x1 + 2 nPml) for its own record length; `cufd` runs each such shot that
+  way and adds its gradient into the full grid at its column offset.
 * `refhost_cufd(...)` runs the reference's own sources compiled for the host
   (oracle/_ref/librefhost_fwi.so, built by oracle/Makefile.refhost); it exists
   only where the reference sources were available at build time.
@@ -100,6 +105,10 @@ def load_shots(survey_fname: str, shot_ids: Sequence[int], if_win: bool) -> list
         shot = {"z_src": int(d["z_src"]), "x_src": int(d["x_src"]), "nrec": int(d["nrec"]),
                 "z_rec": np.asarray(d["z_rec"], dtype=np.int32)[: int(d["nrec"])],
                 "x_rec": np.asarray(d["x_rec"], dtype=np.int32)[: int(d["nrec"])]}
+        if "nSteps" in d:
+            shot["nSteps"] = int(d["nSteps"])
+        if "win_x0" in d:
+            shot["win_x0"], shot["win_x1"] = int(d["win_x0"]), int(d["win_x1"])
         if if_win:
             shot["win_start"] = np.asarray(d["win_start"], dtype=np.float32)
             shot["win_end"] = np.asarray(d["win_end"], dtype=np.float32)
@@ -120,28 +129,9 @@ def _iptr(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
 
 
-def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads: int = 0,
-         obs: Optional[Sequence[np.ndarray]] = None, write_files: bool = True, want_gathers: bool = False,
-         precision: str = "reference") -> dict:
-    """Oracle run of one `cufd` call (libCUFD.cu:34-580).
-
-    lam, mu [MPa] and den are row-major float64 [nz][nx]; stf is
-    [nShotsTotal][nSteps]. shot_ids are 0-based. For calc_id 0/1 observed data
-    are read from `data_dir_name/Shot<id>.bin` unless `obs` is given; for
-    calc_id 2 the gathers are written there when `write_files`.
-    Returns misfit, g_lambda, g_mu, g_den, g_stf and (optionally) gathers.
-    precision "fp32" runs the FP32-only build (no double promotions).
-    """
-    p = load_para(para_fname)
-    shot_ids = [int(v) for v in np.asarray(shot_ids).ravel()]
-    shots = load_shots(p["survey_fname"], shot_ids, p["if_win"])
-    nz, nx, nt = p["nz"], p["nx"], p["nSteps"]
-    lam = np.ascontiguousarray(lam, dtype=np.float64)
-    mu = np.ascontiguousarray(mu, dtype=np.float64)
-    den = np.ascontiguousarray(den, dtype=np.float64)
-    stf = np.ascontiguousarray(np.atleast_2d(stf), dtype=np.float64)
-    if lam.shape != (nz, nx) or mu.shape != (nz, nx) or den.shape != (nz, nx):
-        raise ValueError(f"model shape must be {(nz, nx)}")
+def _run_group(p: dict, shots: list, ids: Sequence[int], nz: int, nx: int, nt: int, lam, mu, den, stf, calc_id: int,
+               obs, nthreads: int, precision: str):
+    """One oracle_cufd call over shots sharing one grid and record length."""
     para = _Para(nz, nx, nt, p["nPml"], p["nPad"], p["dz"], p["dx"], p["dt"], p["f0"], int(p["if_win"]))
     keep = []
     carr = (_Shot * len(shots))()
@@ -158,9 +148,6 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
     n = len(shots)
     obs_ptrs = (ctypes.POINTER(ctypes.c_float) * max(n, 1))()
     if calc_id in (0, 1):
-        if obs is None:
-            obs = [np.fromfile(os.path.join(p["data_dir_name"], f"Shot{sid}.bin"), dtype=np.float32,
-                               count=s["nrec"] * nt) for sid, s in zip(shot_ids, shots)]
         obs = [np.ascontiguousarray(o, dtype=np.float32).reshape(-1) for o in obs]
         for i, o in enumerate(obs):
             if o.size != shots[i]["nrec"] * nt:
@@ -175,15 +162,74 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
     g_mu = np.zeros((nz, nx))
     g_den = np.zeros((nz, nx))
     g_stf = np.zeros_like(stf)
-    ids = np.asarray(shot_ids, dtype=np.int32)
+    cids = np.asarray(ids, dtype=np.int32)
     rc = _load_oracle(precision).oracle_cufd(
-        ctypes.byref(para), carr, n, _iptr(ids), _dptr(lam), _dptr(mu), _dptr(den), _dptr(stf), int(calc_id),
+        ctypes.byref(para), carr, n, _iptr(cids), _dptr(lam), _dptr(mu), _dptr(den), _dptr(stf), int(calc_id),
         obs_ptrs, syn_ptrs, None, ctypes.byref(misfit), _dptr(g_lam), _dptr(g_mu), _dptr(g_den), _dptr(g_stf),
         int(nthreads))
     if rc != 0:
         raise RuntimeError(f"oracle_cufd failed with status {rc}")
-    out = {"misfit": misfit.value, "g_lambda": g_lam, "g_mu": g_mu, "g_den": g_den, "g_stf": g_stf}
-    gathers = [a.reshape(s["nrec"], nt) for a, s in zip(syn, shots)]
+    return misfit.value, g_lam, g_mu, g_den, g_stf, [a.reshape(s["nrec"], nt) for a, s in zip(syn, shots)]
+
+
+def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads: int = 0,
+         obs: Optional[Sequence[np.ndarray]] = None, write_files: bool = True, want_gathers: bool = False,
+         precision: str = "reference") -> dict:
+    """Oracle run of one `cufd` call (libCUFD.cu:34-580).
+
+    lam, mu [MPa] and den are row-major float64 [nz][nx]; stf is
+    [nShotsTotal][nSteps]. shot_ids are 0-based. For calc_id 0/1 observed data
+    are read from `data_dir_name/Shot<id>.bin` unless `obs` is given; for
+    calc_id 2 the gathers are written there when `write_files`.
+    Returns misfit, g_lambda, g_mu, g_den, g_stf and (optionally) gathers
+    (shot k's gather is [nrec][its record length]).
+    precision "fp32" runs the FP32-only build (no double promotions).
+    """
+    p = load_para(para_fname)
+    shot_ids = [int(v) for v in np.asarray(shot_ids).ravel()]
+    shots = load_shots(p["survey_fname"], shot_ids, p["if_win"])
+    nz, nx, nt = p["nz"], p["nx"], p["nSteps"]
+    lam = np.ascontiguousarray(lam, dtype=np.float64)
+    mu = np.ascontiguousarray(mu, dtype=np.float64)
+    den = np.ascontiguousarray(den, dtype=np.float64)
+    stf = np.ascontiguousarray(np.atleast_2d(stf), dtype=np.float64)
+    if lam.shape != (nz, nx) or mu.shape != (nz, nx) or den.shape != (nz, nx):
+        raise ValueError(f"model shape must be {(nz, nx)}")
+    if calc_id in (0, 1) and obs is None:
+        obs = [np.fromfile(os.path.join(p["data_dir_name"], f"Shot{sid}.bin"), dtype=np.float32,
+                           count=s["nrec"] * s.get("nSteps", nt)) for sid, s in zip(shot_ids, shots)]
+    extended = any("nSteps" in s or "win_x0" in s for s in shots)
+    if not extended:
+        misfit, g_lam, g_mu, g_den, g_stf, gathers = _run_group(p, shots, shot_ids, nz, nx, nt, lam, mu, den, stf,
+                                                                calc_id, obs, nthreads, precision)
+    else:
+        # Each shot alone on its sub-model, for its own record length.
+        misfit = 0.0
+        g_lam, g_mu, g_den = np.zeros((nz, nx)), np.zeros((nz, nx)), np.zeros((nz, nx))
+        g_stf = np.zeros_like(stf)
+        gathers = []
+        nPml = p["nPml"]
+        for k, (sid, s) in enumerate(zip(shot_ids, shots)):
+            ntk = s.get("nSteps", nt)
+            x0 = s.get("win_x0", 0)
+            x1 = s.get("win_x1", nx - 2 * nPml - 1)
+            cols = slice(x0, x1 + 1 + 2 * nPml)
+            sub = dict(s)
+            sub["x_src"] = s["x_src"] - x0
+            sub["x_rec"] = np.asarray(s["x_rec"], dtype=np.int32) - x0
+            nxk = x1 - x0 + 1 + 2 * nPml
+            stf_k = np.ascontiguousarray(stf[sid:sid + 1, :ntk])
+            ob = None if obs is None else [obs[k]]
+            m, gl, gm, gd, gs, gth = _run_group(p, [sub], [0], nz, nxk, ntk, np.ascontiguousarray(lam[:, cols]),
+                                               np.ascontiguousarray(mu[:, cols]), np.ascontiguousarray(den[:, cols]),
+                                               stf_k, calc_id, ob, nthreads, precision)
+            misfit += m
+            g_lam[:, cols] += gl
+            g_mu[:, cols] += gm
+            g_den[:, cols] += gd
+            g_stf[sid, :ntk] += gs[0]
+            gathers += gth
+    out = {"misfit": misfit, "g_lambda": g_lam, "g_mu": g_mu, "g_den": g_den, "g_stf": g_stf}
     if calc_id == 2 and write_files:
         for sid, a in zip(shot_ids, gathers):
             a.astype(np.float32).tofile(os.path.join(p["data_dir_name"], f"Shot{sid}.bin"))
