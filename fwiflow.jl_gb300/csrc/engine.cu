@@ -372,6 +372,7 @@ struct ShotPlan {
   size_t taper_off = 0; // floats: 2 * nSteps, or 2 * nrec * nSteps with per-trace windows
   size_t gstf_off = 0;  // floats: nSteps
   size_t cpmlx_off = 0; // floats: 6 * nx (CPML x profiles of the sub-grid)
+  int rbz0 = 0, rbz1 = 0, rbx0 = 0, rbx1 = 0;  // receivers + source bounding box
 };
 
 }  // namespace fwigb
@@ -414,6 +415,8 @@ struct fwigb_ctx {
   std::vector<SweepPack<1>> pack1;
   std::vector<SweepPack<kPackShots>> packs;
   std::vector<int> pack_nx;
+  // Launch extents per pack.
+  std::vector<SweepGrid> pack_grid;
   int last_groups = 0;
   bool model_set = false;
   int last_calc = -1;
@@ -465,7 +468,13 @@ MediaD media_view(fwigb_ctx* ctx, int x_off) {
 
 // Geometry of a grid of width nx (the full grid or a shot's sub-grid) with
 // the CPML profiles az/azh (z) and ax/axh (x) of that grid.
-Geo make_geo(const Params& p, int nx, const float* az, const float* azh, const float* ax, const float* axh) {
+// Geometry of a (sub-)grid of width nx. zprof / xprof are the CPML profile
+// blocks (K, a, b, K_half, a_half, b_half; nz resp. nx floats each).
+Geo make_geo(const Params& p, int nx, const float* zprof, const float* xprof) {
+  const float* az = zprof + p.nz;
+  const float* azh = zprof + 4 * p.nz;
+  const float* ax = xprof + nx;
+  const float* axh = xprof + 4 * nx;
   Geo g{};
   g.nz = p.nz;
   g.nx = nx;
@@ -506,6 +515,41 @@ Geo make_geo(const Params& p, int nx, const float* az, const float* azh, const f
   };
   band(az, azh, p.nz - p.nPad, g.zband_lo, g.zband_hi);
   band(ax, axh, nx, g.xband_lo, g.xband_hi);
+  // Fast box: the longest run of indices where every condition of the fast
+  // sweeps holds (an empty box when none does).
+  auto run = [](int n, auto ok, int& lo, int& hi) {
+    lo = 1;
+    hi = 0;
+    int best = 0;
+    for (int i = 0; i < n;) {
+      if (!ok(i)) {
+        ++i;
+        continue;
+      }
+      int j = i;
+      while (j + 1 < n && ok(j + 1)) ++j;
+      if (j - i + 1 > best) {
+        best = j - i + 1;
+        lo = i;
+        hi = j;
+      }
+      i = j + 1;
+    }
+  };
+  const float* Kz = zprof;
+  const float* Kzh = zprof + 3 * p.nz;
+  const float* Kx = xprof;
+  const float* Kxh = xprof + 3 * nx;
+  run(p.nz, [&](int z) {
+    return z >= g.zs0 && z <= g.zs1 && z >= g.nPml && z <= g.zpml_hi && z > g.zband_lo && z < g.zband_hi &&
+           z >= g.zi0 + 1 && z <= g.zi1 && z >= g.rz0 + 5 && z <= g.rz1 - 5 && Kz[z] == 1.0f && Kzh[z] == 1.0f &&
+           az[z] == 0.0f && azh[z] == 0.0f;
+  }, g.fz0, g.fz1);
+  run(nx, [&](int x) {
+    return x >= g.xs0 && x <= g.xs1 && x >= g.nPml && x <= g.xpml_hi_s && x <= g.xpml_hi_v && x > g.xband_lo &&
+           x < g.xband_hi && x >= g.xi0 + 1 && x <= g.xi1 && x >= g.rx0 + 5 && x <= g.rx1 - 5 && Kx[x] == 1.0f &&
+           Kxh[x] == 1.0f && ax[x] == 0.0f && axh[x] == 0.0f;
+  }, g.fx0, g.fx1);
   return g;
 }
 
@@ -520,7 +564,7 @@ int setup_geometry(fwigb_ctx* ctx) {
                z + 5 * p.nz);
   cpml_profile(p.nx, p.nx, p.nPml, p.dx, p.f0, p.dt, x, x + p.nx, x + 2 * p.nx, x + 3 * p.nx, x + 4 * p.nx,
                x + 5 * p.nx);
-  ctx->geo = make_geo(p, p.nx, z + p.nz, z + 4 * p.nz, x + p.nx, x + 4 * p.nx);
+  ctx->geo = make_geo(p, p.nx, z, x);
   ctx->cells = static_cast<size_t>(ctx->geo.ldz) * p.nx;
   ctx->ncell = static_cast<size_t>(p.nz) * p.nx;
   CK(ctx->cpml.ensure(h.size() * sizeof(float)));
@@ -659,7 +703,7 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
     float* x = hcpml.data() + pl.cpmlx_off;
     cpml_profile(pl.nx, pl.nx, p.nPml, p.dx, p.f0, p.dt, x, x + pl.nx, x + 2 * pl.nx, x + 3 * pl.nx, x + 4 * pl.nx,
                  x + 5 * pl.nx);
-    pl.g = make_geo(p, pl.nx, zprof + p.nz, zprof + 4 * p.nz, x + pl.nx, x + 4 * pl.nx);
+    pl.g = make_geo(p, pl.nx, zprof, x);
     // Source: taper 0.001 (Src_Rec.cu:140) and the add_source scale (utilities.cu:528-538).
     std::vector<float> w(nt);
     if (!taper_weights(nt, p.dt, 0.001f, w.data())) {
@@ -679,10 +723,17 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
     int* off = hblk.data() + pl.blk_off;
     int* lst = off + pl.nbin + 1;
     std::vector<int> cnt(pl.nbin + 1, 0);
+    // Bounding box of the receivers and the source (sub-grid cells).
+    pl.rbz0 = pl.rbz1 = g.z_src;
+    pl.rbx0 = pl.rbx1 = g.x_src - pl.x_off;
     for (int r = 0; r < pl.nrec; ++r) {
       rz[r] = g.z_rec[r];
       rx[r] = g.x_rec[r] - pl.x_off;
       cnt[(rz[r] / kBinZ) + (rx[r] / kBinX) * pl.nbin_z + 1]++;
+      pl.rbz0 = std::min(pl.rbz0, rz[r]);
+      pl.rbz1 = std::max(pl.rbz1, rz[r]);
+      pl.rbx0 = std::min(pl.rbx0, rx[r]);
+      pl.rbx1 = std::max(pl.rbx1, rx[r]);
     }
     for (int b = 0; b < pl.nbin; ++b) cnt[b + 1] += cnt[b];
     for (int b = 0; b <= pl.nbin; ++b) off[b] = cnt[b];
@@ -806,24 +857,21 @@ int plan_groups(fwigb_ctx* ctx, bool adj, std::vector<std::vector<int>>& groups)
 // launches.
 int launch_sweep(fwigb_ctx* ctx, int w, int tx, int a, int arg, bool save, unsigned* d_err) {
   cudaStream_t s = ctx->stream;
-  const int nz = ctx->p.nz;
   const size_t base = static_cast<size_t>(w * 3 + tx_slot(tx));
-  auto go = [&](const auto& pk, int n, int nx) {
+  auto go = [&](const auto& pk, int n, const SweepGrid& gr) {
     switch (w) {
-      case 0: launch_fwd_stress(s, tx, pk, n, nz, nx, arg, save, d_err); break;
-      case 1: launch_fwd_velocity(s, tx, pk, n, nz, nx, d_err); break;
-      case 2: launch_bwd_B(s, tx, pk, n, nz, nx, arg, d_err); break;
-      default: launch_bwd_C(s, tx, pk, n, nz, nx, arg, d_err); break;
+      case 0: return launch_fwd_stress(s, tx, pk, n, gr, arg, save, d_err);
+      case 1: return launch_fwd_velocity(s, tx, pk, n, gr, d_err);
+      case 2: return launch_bwd_B(s, tx, pk, n, gr, arg, d_err);
+      default: return launch_bwd_C(s, tx, pk, n, gr, arg, d_err);
     }
   };
   if (a <= 0) return 0;
-  if (ctx->group_size == 1) {
-    go(ctx->pack1[base], 1, ctx->pack_nx[0]);
-    return 1;
-  }
+  const SweepGrid* grids = ctx->pack_grid.data();
+  if (ctx->group_size == 1) return go(ctx->pack1[base], 1, grids[0]);
   int n = 0;
-  for (int q = 0; q * kPackShots < a; ++q, ++n)
-    go(ctx->packs[base * ctx->npacks + q], std::min(kPackShots, a - q * kPackShots), ctx->pack_nx[q]);
+  for (int q = 0; q * kPackShots < a; ++q)
+    n += go(ctx->packs[base * ctx->npacks + q], std::min(kPackShots, a - q * kPackShots), grids[q]);
   return n;
 }
 
@@ -865,6 +913,10 @@ int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
     sh.blk_off = ctx->shot_blk.as<int>(pl.blk_off);
     sh.blk_rec = sh.blk_off + pl.nbin + 1;
     sh.nbin_z = pl.nbin_z;
+    sh.rbz0 = pl.rbz0;
+    sh.rbz1 = pl.rbz1;
+    sh.rbx0 = pl.rbx0;
+    sh.rbx1 = pl.rbx1;
     const size_t per = static_cast<size_t>(pl.nrec) * pl.nSteps;
     sh.data = ctx->shot_data.as<float>(pl.data_off + per);
     sh.res = ctx->shot_data.as<float>(pl.data_off + 2 * per);
@@ -891,6 +943,8 @@ int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
   ctx->npacks = (G + kPackShots - 1) / kPackShots;
   ctx->pack_nx.assign(ctx->npacks, 0);
   for (int k = 0; k < G; ++k) ctx->pack_nx[k / kPackShots] = std::max(ctx->pack_nx[k / kPackShots], slots[k].g.nx);
+  ctx->pack_grid.assign(ctx->npacks, SweepGrid{ctx->p.nz, 0});
+  for (int q = 0; q < ctx->npacks; ++q) ctx->pack_grid[q].nx = ctx->pack_nx[q];
   if (G == 1) {
     ctx->pack1.assign(12, SweepPack<1>{});
     for (int w = 0; w < 12; ++w) {

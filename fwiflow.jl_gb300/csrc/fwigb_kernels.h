@@ -27,7 +27,7 @@ constexpr int kBoxZ = kTileZ + 8;
 constexpr int kTileXs[3] = {4, 8, 16};
 
 // Tensor maps of the (up to 5) arrays a sweep stages into shared memory.
-struct alignas(64) TileMaps {
+struct TileMaps {  // 128-byte aligned (CUtensorMap)
   CUtensorMap t[5];
 };
 
@@ -45,8 +45,33 @@ struct Geo {
   // Boundary ring saved each forward step: box [rz0,rz1]x[rx0,rx1] minus its
   // inner box shrunk by 5 (the 5 layers around the interior, Boundary.cu:17-27).
   int rz0, rz1, rx0, rx1, ringW, ringH, ring_len;
+  // Fast box (inclusive cell ranges): cells where every sweep reduces to its
+  // interior form. Inside the stencil domain and the reverse-time interior
+  // (with the z-1 / x-1 neighbours of the imaging gathers), outside the CPML,
+  // the adjoint memory bands and the boundary ring, and with K = 1, a = 0 in
+  // both CPML profiles. Empty when fz0 > fz1 or fx0 > fx1.
+  int fz0, fz1, fx0, fx1;
   float dt, rdz, rdx;
 };
+
+// Split of a sub-grid's tiles (32 depths x tx columns, ntz x ntx in all)
+// into the fast tiles, the rectangle [ftz0, ftz1) x [ftx0, ftx1) of tiles
+// inside the fast box, and the edge tiles around it.
+struct TileSplit {
+  int ntz, ntx, ftz0, ftz1, ftx0, ftx1;
+};
+
+__host__ __device__ inline TileSplit tile_split(const Geo& g, int tx) {
+  TileSplit s;
+  s.ntz = (g.nz + kTileZ - 1) / kTileZ;
+  s.ntx = (g.nx + tx - 1) / tx;
+  s.ftz0 = (g.fz0 + kTileZ - 1) / kTileZ;
+  s.ftz1 = (g.fz1 + 1) / kTileZ;
+  s.ftx0 = (g.fx0 + tx - 1) / tx;
+  s.ftx1 = (g.fx1 + 1) / tx;
+  if (g.fz0 > g.fz1 || g.fx0 > g.fx1 || s.ftz1 <= s.ftz0 || s.ftx1 <= s.ftx0) s.ftz0 = s.ftz1 = s.ftx0 = s.ftx1 = 0;
+  return s;
+}
 
 struct Fields {
   float *vz, *vx, *szz, *sxx, *sxz;
@@ -81,6 +106,7 @@ struct ShotD {
   const int* blk_off;     // receivers per 32 x 8 bin (CSR over the bins)
   const int* blk_rec;
   int nbin_z;             // bins along z
+  int rbz0, rbz1, rbx0, rbx1;  // bounding box (cells) of the receivers and the source
   float* data;            // synthetic gathers [nrec][nSteps]
   const float* res;       // adjoint source [nrec][nSteps]
   float* gstf;            // source-time-function gradient [nSteps]
@@ -125,7 +151,7 @@ struct SweepMaps {
 // keeps the parameter block under the 32 KB kernel-parameter limit.
 constexpr int kPackShots = 16;
 template <int K>
-struct alignas(64) SweepPack {
+struct SweepPack {
   TileMaps maps[K];
   ShotSlot slots[K];
 };
@@ -135,23 +161,30 @@ static_assert(sizeof(SweepPack<kPackShots>) < 32000, "sweep pack exceeds the ker
 // cuTensorMapEncodeTiled). Returns false with a message on failure.
 bool encode_sweep_maps(const Geo& g, const Fields& f, int tx, SweepMaps& out, const char** err);
 
+// Launch extent of one sweep over the first shots of a pack: the largest
+// sub-grid among them (nz x nx cells). Blocks past a shot's own grid leave
+// at once.
+struct SweepGrid {
+  int nz, nx;
+};
+
 // ---- launchers (kernels.cu). One launch covers the first `nshots` (<= K)
-// shots of a pack. nx_max is the widest sub-grid among them. err is a device
-// word that a sweep sets when a bounded wait for its staged tiles gives up.
-// The backward sweeps take the backward iteration j; shot k works on its step
-// nSteps_k - 2 - j. Instantiated for K = 1 and K = kPackShots.
+// shots of a pack. err is a device word that a sweep sets when a bounded
+// wait for its staged tiles gives up. The backward sweeps take the backward
+// iteration j; shot k works on its step nSteps_k - 2 - j. Instantiated for
+// K = 1 and K = kPackShots. Each returns the number of kernels it launched.
 template <int K>
-void launch_fwd_stress(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max, int it,
-                       bool save, unsigned* err);
+int launch_fwd_stress(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int it,
+                      bool save, unsigned* err);
 template <int K>
-void launch_fwd_velocity(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max,
-                         unsigned* err);
+int launch_fwd_velocity(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
+                        unsigned* err);
 template <int K>
-void launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max, int j,
-                  unsigned* err);
+int launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
+                 unsigned* err);
 template <int K>
-void launch_bwd_C(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max, int j,
-                  unsigned* err);
+int launch_bwd_C(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
+                 unsigned* err);
 // Adds the per-shot gradients of the first nshots slots into the global ones.
 void launch_reduce_grads(cudaStream_t s, int nz, int nx, int ldz, int nshots, const ShotSlot* slots, float* g_lam,
                          float* g_mu, float* g_den);

@@ -139,22 +139,43 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
   return make_int2(sh.blk_off[b], sh.blk_off[b + 1]);
 }
 
-// Every sweep is launched once per time step for a group of shots: blockIdx.z
-// is the shot (its slot holds its sub-grid, fields, source, receivers and
-// TMA maps), blockIdx.x / blockIdx.y the tile of 32 depths x TX columns. The
-// launch covers the group's widest shot; blocks past a narrower shot's grid
-// leave before staging anything. Block (32, TX), one cell per thread: lane
-// threadIdx.x is the depth offset, threadIdx.y the column offset; `b` is the
-// cell's index in a staged box (column stride kBoxZ).
-#define SWEEP_SETUP(NA)                                                        \
+// Every sweep is one launch per time step for a pack of shots: blockIdx.z is
+// the shot (its slot holds its sub-grid, fields, source, receivers and TMA
+// maps), blockIdx.x / blockIdx.y the tile of 32 depths x TX columns. A tile
+// inside the shot's fast rectangle runs the sweep's fast body (the interior
+// form of the reference kernels); any other tile runs its edge body (the
+// full CPML / boundary-ring / band logic). The choice is uniform per block.
+// Blocks past a narrower shot's grid leave before staging anything. Block
+// (32, TX), one cell per thread: lane threadIdx.x is the depth offset,
+// threadIdx.y the column offset; `b` is the cell's index in a staged box
+// (column stride kBoxZ).
+#define SWEEP_KERNEL_TILE()                                                    \
+  const int shot = K == 1 ? 0 : static_cast<int>(blockIdx.z);                  \
+  const Geo& g0 = P.slots[shot].g;                                             \
+  const int z0 = blockIdx.x * kTileZ, x0 = blockIdx.y * TX;                    \
+  if (z0 >= g0.nz || x0 >= g0.nx) return;                                      \
+  const TileSplit ts = tile_split(g0, TX);                                     \
+  const bool fast = static_cast<int>(blockIdx.x) >= ts.ftz0 &&                 \
+                    static_cast<int>(blockIdx.x) < ts.ftz1 &&                  \
+                    static_cast<int>(blockIdx.y) >= ts.ftx0 &&                 \
+                    static_cast<int>(blockIdx.y) < ts.ftx1;
+
+#define SWEEP_BODY_SLOT()                                                      \
+  const ShotSlot& S = P.slots[shot];                                           \
+  const Geo& g = S.g;
+
+// A fast tile lies wholly inside the grid. `special` marks the tiles that
+// meet the bounding box of the shot's receivers and source.
+#define SWEEP_FAST_SLOT()                                                      \
+  SWEEP_BODY_SLOT()                                                            \
+  const ShotD& sh = S.sh;                                                      \
+  const bool special = !(z0 + kTileZ - 1 < sh.rbz0 || z0 > sh.rbz1 ||          \
+                         x0 + TX - 1 < sh.rbx0 || x0 > sh.rbx1);
+
+#define SWEEP_STAGE(NA)                                                        \
   constexpr int N = kBoxZ * (TX + 4);                                          \
   extern __shared__ __align__(128) float sm[];                                 \
   __shared__ __align__(8) uint64_t bar;                                        \
-  const int shot = K == 1 ? 0 : static_cast<int>(blockIdx.z);                  \
-  const ShotSlot& S = P.slots[shot];                                           \
-  const Geo& g = S.g;                                                          \
-  const int z0 = blockIdx.x * kTileZ, x0 = blockIdx.y * TX;                    \
-  if (z0 >= g.nz || x0 >= g.nx) return; /* block-uniform */                    \
   stage_begin<NA, TX>(P.maps[shot], sm, &bar, z0, x0);                         \
   const Fields& f = S.f;                                                       \
   const MediaD& m = S.m;                                                       \
@@ -180,8 +201,9 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
 // recording (utilities.cu:557-567) + from_bnd of the 5 fields (Boundary.cu:55-76).
 // Staged: vz, vx.
 template <int TX, int K>
-__global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ SweepPack<K> P, int it, int save, unsigned* err) {
-  SWEEP_SETUP(2)
+__device__ __forceinline__ void fwd_stress_edge(const SweepPack<K>& P, int shot, int z0, int x0, int it, int save, unsigned* err) {
+  SWEEP_BODY_SLOT()
+  SWEEP_STAGE(2)
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
   float szz = f.szz[i], sxx = f.sxx[i], sxz = f.sxz[i];
@@ -246,8 +268,9 @@ __global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ SweepPack<K> P, 
 
 // F2: el_velocity, isFor = true (el_velocity.cu:45-82). Staged: szz, sxx, sxz.
 template <int TX, int K>
-__global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ SweepPack<K> P, unsigned* err) {
-  SWEEP_SETUP(3)
+__device__ __forceinline__ void fwd_velocity_edge(const SweepPack<K>& P, int shot, int z0, int x0, unsigned* err) {
+  SWEEP_BODY_SLOT()
+  SWEEP_STAGE(3)
   const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
   float vz = 0.0f, vx = 0.0f, bA = 0.0f, bB = 0.0f;
   if (dom) {
@@ -288,8 +311,9 @@ __global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ SweepPack<K> P
 // B: add_source(-) + el_stress(isFor=false) with the lambda / mu kernels +
 // to_bnd(stress) + el_velocity_adj. Staged: vz, vx, szz_a, sxx_a, sxz_a.
 template <int TX, int K>
-__global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
-  SWEEP_SETUP(5)
+__device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
+  SWEEP_BODY_SLOT()
+  SWEEP_STAGE(5)
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
   const Grads& gr = S.gr;
@@ -405,8 +429,9 @@ __global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ SweepPack<K> P, int j
 //    density kernel (el_velocity.cu:220-244) + to_bnd(velocity).
 //    Staged: vz_a, vx_a, szz, sxx, sxz.
 template <int TX, int K>
-__global__ void BWD_BOUNDS k_bwd_C(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
-  SWEEP_SETUP(5)
+__device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
+  SWEEP_BODY_SLOT()
+  SWEEP_STAGE(5)
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
   const Grads& gr = S.gr;
@@ -519,6 +544,245 @@ __global__ void BWD_BOUNDS k_bwd_C(const __grid_constant__ SweepPack<K> P, int j
     }
     gr.den[i] = acc;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Fast-tile forms of the four sweeps. Every cell of a fast tile is in the
+// stencil domain and the reverse-time interior, outside the CPML, the
+// adjoint memory bands and the boundary ring, with K = 1 and a = 0: the
+// reference's CPML divisions by K are exact there (x / 1 = x) and are left
+// out, the memory-array updates and the ring are never reached, and the
+// source / receiver terms are evaluated only in tiles that meet the bounding
+// box of the shot's receivers and source. Operation order otherwise follows
+// the edge kernels.
+
+template <int TX, int K>
+__device__ __forceinline__ void fwd_stress_fast(const SweepPack<K>& P, int shot, int z0, int x0, int it, unsigned* err) {
+  SWEEP_FAST_SLOT()
+  SWEEP_STAGE(2)
+  float szz = f.szz[i], sxx = f.sxx[i];
+  const float sxz = f.sxz[i];
+  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
+  if (!stage_wait(&bar, err)) return;
+  const float* s_vz = sm;
+  const float* s_vx = sm + N;
+  const float dvz_dz = sdm(s_vz, b, 1, g.rdz);
+  const float dvx_dx = sdm(s_vx, b, kBoxZ, g.rdx);
+  const float dvx_dz = sdp(s_vx, b, 1, g.rdz);
+  const float dvz_dx = sdp(s_vz, b, kBoxZ, g.rdx);
+  szz += (l2m * dvz_dz + lam * dvx_dx) * g.dt;
+  sxx += (lam * dvz_dz + l2m * dvx_dx) * g.dt;
+  f.sxz[i] = sxz + amu * (dvx_dz + dvz_dx) * g.dt;
+  if (special) {
+    if (z == sh.src_z && x == sh.src_x) {
+      szz += sh.src_szz[it];
+      sxx += sh.src_sxx[it];
+    }
+    const int2 rr = bin_range(sh, z, x);
+    for (int k = rr.x; k < rr.y; ++k) {
+      const int r = sh.blk_rec[k];
+      if (sh.rec_z[r] == z && sh.rec_x[r] == x)
+        sh.data[static_cast<size_t>(r) * sh.nSteps + it + 1] = szz + 3.0f * sxx;
+    }
+  }
+  f.szz[i] = szz;
+  f.sxx[i] = sxx;
+}
+
+template <int TX, int K>
+__device__ __forceinline__ void fwd_velocity_fast(const SweepPack<K>& P, int shot, int z0, int x0, unsigned* err) {
+  SWEEP_FAST_SLOT()
+  (void)special;
+  SWEEP_STAGE(3)
+  const float vz = f.vz[i], vx = f.vx[i], bA = m.bycA[i], bB = m.bycB[i];
+  if (!stage_wait(&bar, err)) return;
+  const float* s_szz = sm;
+  const float* s_sxx = sm + N;
+  const float* s_sxz = sm + 2 * N;
+  const float dszz_dz = sdp(s_szz, b, 1, g.rdz);
+  const float dsxz_dx = sdm(s_sxz, b, kBoxZ, g.rdx);
+  const float dsxz_dz = sdm(s_sxz, b, 1, g.rdz);
+  const float dsxx_dx = sdp(s_sxx, b, kBoxZ, g.rdx);
+  f.vz[i] = vz + (dszz_dz + dsxz_dx) * bA * g.dt;
+  f.vx[i] = vx + (dsxz_dz + dsxx_dx) * bB * g.dt;
+}
+
+template <int TX, int K>
+__device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
+  SWEEP_FAST_SLOT()
+  SWEEP_STAGE(5)
+  const Grads& gr = S.gr;
+  const int it = S.nSteps - 2 - j;
+  const float dt = g.dt;
+  float szz = f.szz[i], sxx = f.sxx[i], sxz = f.sxz[i];
+  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
+  const float gl = gr.lam[i], gm = gr.mu[i], w = m.muw[i], h = m.hs[i];
+  const float va_z = f.vz_a[i], va_x = f.vx_a[i];
+  const float hz = m.hs[i - 1], hx = m.hs[i - ldz], hzx = m.hs[i - ldz - 1];
+  if (!stage_wait(&bar, err)) return;
+  const float* s_vz = sm;
+  const float* s_vx = sm + N;
+  const float* s_szz_a = sm + 2 * N;
+  const float* s_sxx_a = sm + 3 * N;
+  const float* s_sxz_a = sm + 4 * N;
+  if (special && z == sh.src_z && x == sh.src_x) {
+    szz -= sh.src_szz[it];
+    sxx -= sh.src_sxx[it];
+  }
+  const float dvz_dz = sdm(s_vz, b, 1, g.rdz);
+  const float dvx_dx = sdm(s_vx, b, kBoxZ, g.rdx);
+  const float dvx_dz = sdp(s_vx, b, 1, g.rdz);
+  const float dvz_dx = sdp(s_vz, b, kBoxZ, g.rdx);
+  szz -= (l2m * dvz_dz + lam * dvx_dx) * dt;
+  sxx -= (lam * dvz_dz + l2m * dvx_dx) * dt;
+  const float e_own = dvx_dz + dvz_dx;
+  sxz -= amu * e_own * dt;
+  const float sa = s_szz_a[b], xa = s_sxx_a[b];
+  gr.lam[i] = gl + -(sa + xa) * (dvz_dz + dvx_dx) * dt * kMega;
+  const float gmu_own = (-2.0f * sa * dvz_dz * dt - 2.0f * xa * dvx_dx * dt) * kMega;
+  f.szz[i] = szz;
+  f.sxx[i] = sxx;
+  f.sxz[i] = sxz;
+  // mu kernel: own term and the three neighbouring 2x2 blocks (all guards hold).
+  float acc = gm + gmu_own;
+  if (h != 0.0f) acc += w * (-s_sxz_a[b] * e_own * dt * h);
+  if (hz != 0.0f) {
+    const int bj = b - 1;
+    acc += w * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, kBoxZ, g.rdx)) * dt * hz);
+  }
+  if (hx != 0.0f) {
+    const int bj = b - kBoxZ;
+    acc += w * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, kBoxZ, g.rdx)) * dt * hx);
+  }
+  if (hzx != 0.0f) {
+    const int b2 = b - kBoxZ - 1;
+    acc += w * (-s_sxz_a[b2] * (sdp(s_vx, b2, 1, g.rdz) + sdp(s_vz, b2, kBoxZ, g.rdx)) * dt * hzx);
+  }
+  gr.mu[i] = acc;
+  // el_velocity_adj without the psi memory terms.
+  {
+    const float dszz_dx = -sdp(s_szz_a, b, kBoxZ, g.rdx);
+    const float dsxx_dx = -sdp(s_sxx_a, b, kBoxZ, g.rdx);
+    const float dsxz_dz = -sdm(s_sxz_a, b, 1, g.rdz);
+    f.vx_a[i] = va_x + (lam * dszz_dx * dt + l2m * dsxx_dx * dt + amu * dsxz_dz * dt);
+  }
+  {
+    const float dszz_dz = -sdp(s_szz_a, b, 1, g.rdz);
+    const float dsxx_dz = -sdp(s_sxx_a, b, 1, g.rdz);
+    const float dsxz_dx = -sdm(s_sxz_a, b, kBoxZ, g.rdx);
+    f.vz_a[i] = va_z + (l2m * dszz_dz * dt + lam * dsxx_dz * dt + amu * dsxz_dx * dt);
+  }
+}
+
+template <int TX, int K>
+__device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
+  SWEEP_FAST_SLOT()
+  SWEEP_STAGE(5)
+  const Grads& gr = S.gr;
+  const int it = S.nSteps - 2 - j;
+  const int rev = it >= 1;
+  const float dt = g.dt;
+  float sa = f.szz_a[i], xa = f.sxx_a[i], za = f.sxz_a[i];
+  const float bA = m.bycA[i], bB = m.bycB[i];
+  float vz = 0.0f, vx = 0.0f, gd = 0.0f, bAj = 0.0f, bBj = 0.0f;
+  if (rev) {
+    vz = f.vz[i];
+    vx = f.vx[i];
+    gd = gr.den[i];
+    bAj = m.bycA[i - 1];
+    bBj = m.bycB[i - ldz];
+  }
+  if (!stage_wait(&bar, err)) return;
+  const float* s_vz_a = sm;
+  const float* s_vx_a = sm + N;
+  const float* s_szz = sm + 2 * N;
+  const float* s_sxx = sm + 3 * N;
+  const float* s_sxz = sm + 4 * N;
+  if (special) {
+    const int2 rr = bin_range(sh, z, x);
+    for (int k = rr.x; k < rr.y; ++k) {
+      const int r = sh.blk_rec[k];
+      if (sh.rec_z[r] == z && sh.rec_x[r] == x) {
+        const float rv = sh.res[static_cast<size_t>(r) * sh.nSteps + it];
+        sa += rv;
+        xa += 3.0f * rv;
+      }
+    }
+  }
+  {
+    const float dvz_dx = -sdp(s_vz_a, b, kBoxZ, g.rdx);
+    const float dvx_dz = -sdp(s_vx_a, b, 1, g.rdz);
+    za += dvz_dx * bA * dt + dvx_dz * bB * dt;
+    f.sxz_a[i] = za;
+  }
+  {
+    const float dvx_dx = -sdm(s_vx_a, b, kBoxZ, g.rdx);
+    const float dvz_dz = -sdm(s_vz_a, b, 1, g.rdz);
+    xa += bB * dvx_dx * dt;
+    sa += bA * dvz_dz * dt;
+  }
+  f.szz_a[i] = sa;
+  f.sxx_a[i] = xa;
+  if (!rev) return;
+  if (special && z == sh.src_z && x == sh.src_x) sh.gstf[it - 1] = -(sa + 3.0f * xa) * dt;
+  const float ea = sdp(s_szz, b, 1, g.rdz) + sdm(s_sxz, b, kBoxZ, g.rdx);  // dszz_dz + dsxz_dx
+  const float eb = sdm(s_sxz, b, 1, g.rdz) + sdp(s_sxx, b, kBoxZ, g.rdx);  // dsxz_dz + dsxx_dx
+  f.vz[i] = vz - ea * bA * dt;
+  f.vx[i] = vx - eb * bB * dt;
+  // rho kernel gather (all guards hold).
+  float acc = gd;
+  acc += -s_vz_a[b] * ea * dt * (-bA * bA * 0.5f);
+  acc += -s_vx_a[b] * eb * dt * (-bB * bB * 0.5f);
+  {
+    const int bj = b - 1;
+    const float e = sdp(s_szz, bj, 1, g.rdz) + sdm(s_sxz, bj, kBoxZ, g.rdx);
+    acc += -s_vz_a[bj] * e * dt * (-bAj * bAj * 0.5f);
+  }
+  {
+    const int bj = b - kBoxZ;
+    const float e = sdm(s_sxz, bj, 1, g.rdz) + sdp(s_sxx, bj, kBoxZ, g.rdx);
+    acc += -s_vx_a[bj] * e * dt * (-bBj * bBj * 0.5f);
+  }
+  gr.den[i] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// The sweep kernels: one launch per sweep and time step.
+
+template <int TX, int K>
+__global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ SweepPack<K> P, int it, int save, unsigned* err) {
+  SWEEP_KERNEL_TILE()
+  if (fast)
+    fwd_stress_fast<TX, K>(P, shot, z0, x0, it, err);
+  else
+    fwd_stress_edge<TX, K>(P, shot, z0, x0, it, save, err);
+}
+
+template <int TX, int K>
+__global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ SweepPack<K> P, unsigned* err) {
+  SWEEP_KERNEL_TILE()
+  if (fast)
+    fwd_velocity_fast<TX, K>(P, shot, z0, x0, err);
+  else
+    fwd_velocity_edge<TX, K>(P, shot, z0, x0, err);
+}
+
+template <int TX, int K>
+__global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
+  SWEEP_KERNEL_TILE()
+  if (fast)
+    bwd_B_fast<TX, K>(P, shot, z0, x0, j, err);
+  else
+    bwd_B_edge<TX, K>(P, shot, z0, x0, j, err);
+}
+
+template <int TX, int K>
+__global__ void BWD_BOUNDS k_bwd_C(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
+  SWEEP_KERNEL_TILE()
+  if (fast)
+    bwd_C_fast<TX, K>(P, shot, z0, x0, j, err);
+  else
+    bwd_C_edge<TX, K>(P, shot, z0, x0, j, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -678,68 +942,73 @@ __global__ void k_sum_partials(const double* __restrict__ partials, int n, doubl
 namespace {
 
 template <int TX>
-dim3 sweep_grid(int nz, int nx_max, int nshots) {
-  return dim3((nz + kTileZ - 1) / kTileZ, (nx_max + TX - 1) / TX, nshots);
-}
-template <int TX>
 constexpr size_t smem_bytes(int na) {
   return static_cast<size_t>(na) * kBoxZ * (TX + 4) * sizeof(float);
 }
 
 }  // namespace
 
-#define FWIGB_DISPATCH_TX(tx, CALL) \
-  switch (tx) {                     \
-    case 4: {                       \
-      constexpr int TX = 4;         \
-      CALL;                         \
-      break;                        \
-    }                               \
-    case 8: {                       \
-      constexpr int TX = 8;         \
-      CALL;                         \
-      break;                        \
-    }                               \
-    default: {                      \
-      constexpr int TX = 16;        \
-      CALL;                         \
-      break;                        \
-    }                               \
+#define FWIGB_DISPATCH_TX(tx, ...) \
+  switch (tx) {                    \
+    case 4: {                      \
+      constexpr int TX = 4;        \
+      __VA_ARGS__;                 \
+      break;                       \
+    }                              \
+    case 8: {                      \
+      constexpr int TX = 8;        \
+      __VA_ARGS__;                 \
+      break;                       \
+    }                              \
+    default: {                     \
+      constexpr int TX = 16;       \
+      __VA_ARGS__;                 \
+      break;                       \
+    }                              \
   }
 
-template <int K>
-void launch_fwd_stress(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max, int it,
-                       bool save, unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, (k_fwd_stress<TX, K><<<sweep_grid<TX>(nz, nx_max, nshots), dim3(32, TX), smem_bytes<TX>(2),
-                                              s>>>(p, it, save ? 1 : 0, err)))
+dim3 sweep_grid(int tx, const SweepGrid& gr, int nshots) {
+  return dim3((gr.nz + kTileZ - 1) / kTileZ, (gr.nx + tx - 1) / tx, nshots);
 }
 
 template <int K>
-void launch_fwd_velocity(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max,
-                         unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, (k_fwd_velocity<TX, K><<<sweep_grid<TX>(nz, nx_max, nshots), dim3(32, TX),
-                                                smem_bytes<TX>(3), s>>>(p, err)))
+int launch_fwd_stress(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int it,
+                      bool save, unsigned* err) {
+  FWIGB_DISPATCH_TX(tx, k_fwd_stress<TX, K><<<sweep_grid(TX, gr, nshots), dim3(32, TX), smem_bytes<TX>(2), s>>>(
+                            p, it, save ? 1 : 0, err))
+  return 1;
 }
 
 template <int K>
-void launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max, int j,
-                  unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, (k_bwd_B<TX, K><<<sweep_grid<TX>(nz, nx_max, nshots), dim3(32, TX), smem_bytes<TX>(5), s>>>(
-                            p, j, err)))
+int launch_fwd_velocity(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
+                        unsigned* err) {
+  FWIGB_DISPATCH_TX(tx, k_fwd_velocity<TX, K><<<sweep_grid(TX, gr, nshots), dim3(32, TX), smem_bytes<TX>(3), s>>>(
+                            p, err))
+  return 1;
 }
 
 template <int K>
-void launch_bwd_C(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, int nz, int nx_max, int j,
-                  unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, (k_bwd_C<TX, K><<<sweep_grid<TX>(nz, nx_max, nshots), dim3(32, TX), smem_bytes<TX>(5), s>>>(
-                            p, j, err)))
+int launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
+                 unsigned* err) {
+  FWIGB_DISPATCH_TX(tx, k_bwd_B<TX, K><<<sweep_grid(TX, gr, nshots), dim3(32, TX), smem_bytes<TX>(5), s>>>(p, j,
+                                                                                                         err))
+  return 1;
 }
 
-#define FWIGB_INSTANTIATE(K)                                                                                      \
-  template void launch_fwd_stress<K>(cudaStream_t, int, const SweepPack<K>&, int, int, int, int, bool, unsigned*); \
-  template void launch_fwd_velocity<K>(cudaStream_t, int, const SweepPack<K>&, int, int, int, unsigned*);          \
-  template void launch_bwd_B<K>(cudaStream_t, int, const SweepPack<K>&, int, int, int, int, unsigned*);            \
-  template void launch_bwd_C<K>(cudaStream_t, int, const SweepPack<K>&, int, int, int, int, unsigned*);
+template <int K>
+int launch_bwd_C(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
+                 unsigned* err) {
+  FWIGB_DISPATCH_TX(tx, k_bwd_C<TX, K><<<sweep_grid(TX, gr, nshots), dim3(32, TX), smem_bytes<TX>(5), s>>>(p, j,
+                                                                                                         err))
+  return 1;
+}
+
+#define FWIGB_INSTANTIATE(K)                                                                                    \
+  template int launch_fwd_stress<K>(cudaStream_t, int, const SweepPack<K>&, int, const SweepGrid&, int, bool,    \
+                                    unsigned*);                                                                  \
+  template int launch_fwd_velocity<K>(cudaStream_t, int, const SweepPack<K>&, int, const SweepGrid&, unsigned*); \
+  template int launch_bwd_B<K>(cudaStream_t, int, const SweepPack<K>&, int, const SweepGrid&, int, unsigned*);   \
+  template int launch_bwd_C<K>(cudaStream_t, int, const SweepPack<K>&, int, const SweepGrid&, int, unsigned*);
 FWIGB_INSTANTIATE(1)
 FWIGB_INSTANTIATE(kPackShots)
 #undef FWIGB_INSTANTIATE
