@@ -968,38 +968,43 @@ int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
 }
 
 // Tile-width autotuner: times every width of each sweep on the first group of
-// the first run (a few launches each on its live buffers, which the run then
-// resets) and keeps the fastest. The backward sweeps are tuned on the first
-// run with the adjoint.
+// the first run (on its live buffers, which the run then resets) and keeps
+// the fastest. The widths are timed interleaved over several rounds and each
+// keeps its best time, so a transient on the GPU does not decide the choice.
+// The backward sweeps are tuned on the first run with the adjoint.
 int autotune(fwigb_ctx* ctx, int nshots, int nx_max, bool adj) {
   cudaStream_t s = ctx->stream;
   unsigned* d_err = reinterpret_cast<unsigned*>(ctx->scal.as<char>() + 16);
   (void)nx_max;
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  constexpr int kRounds = 4, kReps = 5;
+  std::vector<cudaEvent_t> ev(2 * kRounds * 3);
+  for (cudaEvent_t& e : ev) CK(cudaEventCreate(&e));
   const int kinds_end = (adj && ctx->nSteps_max >= 2) ? 4 : 2;
   for (int kind = ctx->tuned_fwd ? 2 : 0; kind < kinds_end; ++kind) {
+    for (int slot = 0; slot < 3; ++slot) launch_sweep(ctx, kind, kTileXs[slot], nshots, 0, false, d_err);  // warm-up
+    for (int r = 0; r < kRounds; ++r)
+      for (int slot = 0; slot < 3; ++slot) {
+        CK(cudaEventRecord(ev[2 * (r * 3 + slot)], s));
+        for (int k = 0; k < kReps; ++k) launch_sweep(ctx, kind, kTileXs[slot], nshots, 0, false, d_err);
+        CK(cudaEventRecord(ev[2 * (r * 3 + slot) + 1], s));
+      }
+    CK(cudaStreamSynchronize(s));
     float best = 1e30f;
     for (int slot = 0; slot < 3; ++slot) {
-      const int tx = kTileXs[slot];
-      auto launch = [&]() { launch_sweep(ctx, kind, tx, nshots, 0, false, d_err); };
-      for (int w = 0; w < 2; ++w) launch();
-      CK(cudaEventRecord(e0, s));
-      for (int r = 0; r < 10; ++r) launch();
-      CK(cudaEventRecord(e1, s));
-      CK(cudaEventSynchronize(e1));
-      float ms = 0.0f;
-      CK(cudaEventElapsedTime(&ms, e0, e1));
-      if (ms < best) {
-        best = ms;
-        ctx->tx[kind] = tx;
+      float t = 1e30f;
+      for (int r = 0; r < kRounds; ++r) {
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, ev[2 * (r * 3 + slot)], ev[2 * (r * 3 + slot) + 1]));
+        t = std::min(t, ms);
+      }
+      if (t < best) {
+        best = t;
+        ctx->tx[kind] = kTileXs[slot];
       }
     }
   }
   CK(cudaGetLastError());
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
   ctx->tuned_fwd = true;
   if (kinds_end == 4) ctx->tuned_bwd = true;
   return FWIGB_OK;
