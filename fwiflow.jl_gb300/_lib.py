@@ -60,6 +60,21 @@ SIGNATURES = {
     "fwigb_tile_config": ([_V, _I], ctypes.c_int),
     "fwigb_set_batching": ([_V, ctypes.c_int, ctypes.c_ulonglong], ctypes.c_int),
     "fwigb_last_group_count": ([_V], ctypes.c_int),
+    "fwigb_set_illumination": ([_V, ctypes.c_int], ctypes.c_int),
+    "fwigb_fetch_illumination": ([_V, _D], ctypes.c_int),
+    "fwigb_cnn_conv3x3": ([_V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _V, _V, _V, _V,
+                           _V, _V, _V], ctypes.c_int),
+    "fwigb_cnn_tile_count": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "fwigb_cnn_wgrad_partials": ([_V, _V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _V, _V],
+                                 ctypes.c_int),
+    "fwigb_cnn_reduce_partials": ([_V, ctypes.c_int, ctypes.c_int, _V, _V], ctypes.c_int),
+    "fwigb_cnn_bias_partials": ([_V, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, _V, _V], ctypes.c_int),
+    "fwigb_cnn_adam": ([_V, _V, _V, _V, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                        ctypes.c_float, ctypes.c_int, _V], ctypes.c_int),
+    "fwigb_cnn_pack_weights": ([_V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _V, _V],
+                               ctypes.c_int),
+    "fwigb_cnn_mse_grad": ([_V, _V, _V, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_float, _V, _V, _V],
+                           ctypes.c_int),
     "fwigb_set_tile_config": ([_V, _I], ctypes.c_int),
     "fwigb_kernel_times": ([_V, _D, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
 }

@@ -418,6 +418,8 @@ struct fwigb_ctx {
   // Launch extents per pack.
   std::vector<SweepGrid> pack_grid;
   int last_groups = 0;
+  bool illum = false;       // accumulate the source illumination in the runs
+  bool illum_valid = false; // the last run accumulated it
   bool model_set = false;
   int last_calc = -1;
   long long launches = 0;
@@ -572,7 +574,7 @@ int setup_geometry(fwigb_ctx* ctx) {
   CK(ctx->media.ensure(9 * ctx->cells * sizeof(float)));
   CK(cudaMemset(ctx->media.p, 0, 9 * ctx->cells * sizeof(float)));
   CK(ctx->stage.ensure(3 * ctx->ncell * sizeof(double)));
-  CK(ctx->grads.ensure(3 * ctx->cells * sizeof(float)));
+  CK(ctx->grads.ensure(4 * ctx->cells * sizeof(float)));  // lambda, mu, den, illumination
   // [0]: misfit accumulator (double), [8]: cp max bits, [16]: sweep error word
   CK(ctx->scal.ensure(64));
   CK(cudaMemset(ctx->scal.p, 0, 64));
@@ -817,7 +819,7 @@ int plan_groups(fwigb_ctx* ctx, bool adj, std::vector<std::vector<int>>& groups)
   }
   const size_t ldz = ctx->geo.ldz;
   ctx->fields_stride = 18 * ldz * nx_max;
-  ctx->grads_stride = 3 * ldz * nx_max;
+  ctx->grads_stride = (ctx->illum ? 4 : 3) * ldz * nx_max;
   ctx->store_stride = adj ? static_cast<size_t>(ctx->nSteps_max) * 5 * ring_max : 0;
   const size_t per_member = (ctx->fields_stride + ctx->grads_stride + ctx->store_stride) * sizeof(float);
   size_t budget = ctx->mem_budget;
@@ -923,7 +925,7 @@ int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
     sh.gstf = ctx->shot_gstf.as<float>(pl.gstf_off);
     sl.st = StoreD{ctx->store_stride ? ctx->g_store.as<float>(k * ctx->store_stride) : nullptr};
     float* gb = ctx->g_grads.as<float>(k * ctx->grads_stride);
-    sl.gr = Grads{gb, gb + n, gb + 2 * n};
+    sl.gr = Grads{gb, gb + n, gb + 2 * n, ctx->illum ? gb + 3 * n : nullptr};
     sl.nSteps = pl.nSteps;
     sl.x_off = pl.x_off;
     for (int t = 0; t < 3; ++t) {
@@ -1037,6 +1039,7 @@ int run(fwigb_ctx* ctx, int calc_id) {
   double* d_misfit = ctx->scal.as<double>();
   CK(cudaMemsetAsync(d_misfit, 0, sizeof(double), s));
   if (adj) CK(cudaMemsetAsync(ctx->grads.p, 0, 3 * ctx->cells * sizeof(float), s));
+  if (ctx->illum) CK(cudaMemsetAsync(ctx->grads.as<float>(3 * ctx->cells), 0, ctx->cells * sizeof(float), s));
   long long launches = 0;
   ctx->ev_kind.clear();
   size_t ev_used = 0;
@@ -1083,7 +1086,8 @@ int run(fwigb_ctx* ctx, int calc_id) {
       CK(cudaMemsetAsync(ctx->shot_data.as<float>(pl.data_off + per), 0, per * sizeof(float), s));
       if (adj) CK(cudaMemsetAsync(ctx->shot_gstf.as<float>(pl.gstf_off), 0, pl.nSteps * sizeof(float), s));
     }
-    if (adj) CK(cudaMemsetAsync(ctx->g_grads.p, 0, static_cast<size_t>(G) * ctx->grads_stride * sizeof(float), s));
+    if (adj || ctx->illum)
+      CK(cudaMemsetAsync(ctx->g_grads.p, 0, static_cast<size_t>(G) * ctx->grads_stride * sizeof(float), s));
     const int ntop = nst[0];
     for (int it = 0; it <= ntop - 2; ++it) {
       const int a = active(it);
@@ -1123,8 +1127,11 @@ int run(fwigb_ctx* ctx, int calc_id) {
         TIMED(2, launches += launch_sweep(ctx, 2, ctx->tx[2], a, j, false, d_err));
         TIMED(3, launches += launch_sweep(ctx, 3, ctx->tx[3], a, j, false, d_err));
       }
+    }
+    if (adj || ctx->illum) {
       float* gb = ctx->grads.as<float>();
-      launch_reduce_grads(s, nz, ctx->p.nx, ctx->geo.ldz, G, slots, gb, gb + ctx->cells, gb + 2 * ctx->cells);
+      launch_reduce_grads(s, nz, ctx->p.nx, ctx->geo.ldz, G, slots, adj ? gb : nullptr, gb + ctx->cells,
+                          gb + 2 * ctx->cells, ctx->illum ? gb + 3 * ctx->cells : nullptr);
       ++launches;
     }
     // The next group reuses the slots and maps; wait for this one.
@@ -1135,6 +1142,7 @@ int run(fwigb_ctx* ctx, int calc_id) {
   ctx->launches = launches;
   ctx->last_calc = calc_id;
   ctx->last_groups = static_cast<int>(groups.size());
+  ctx->illum_valid = ctx->illum;
   return FWIGB_OK;
 }
 
@@ -1393,6 +1401,28 @@ int fwigb_set_batching(fwigb_ctx* ctx, int max_shots, unsigned long long mem_bud
 }
 
 int fwigb_last_group_count(const fwigb_ctx* ctx) { return ctx ? ctx->last_groups : -1; }
+
+int fwigb_set_illumination(fwigb_ctx* ctx, int enable) {
+  if (!ctx) return FWIGB_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->illum = enable != 0;
+  return FWIGB_OK;
+}
+
+int fwigb_fetch_illumination(fwigb_ctx* ctx, double* illum) {
+  if (!ctx || !illum) return FWIGB_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!ctx->illum_valid) {
+    ctx->err = "the last run did not accumulate the illumination (fwigb_set_illumination)";
+    return FWIGB_ERR_ARG;
+  }
+  cudaStream_t s = ctx->stream;
+  double* st = ctx->stage.as<double>();
+  launch_to_rowmajor(s, ctx->p.nz, ctx->p.nx, ctx->geo.ldz, ctx->grads.as<float>(3 * ctx->cells), st, 1.0);
+  CK(cudaMemcpyAsync(illum, st, ctx->ncell * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return FWIGB_OK;
+}
 
 int fwigb_set_kernel_timing(fwigb_ctx* ctx, int enable) {
   if (!ctx) return FWIGB_ERR_ARG;

@@ -120,6 +120,7 @@ struct Grads {
   float* lam;
   float* mu;
   float* den;
+  float* illum;  // source illumination sum_t (vz^2 + vx^2), or null when not accumulated
 };
 
 // Everything one shot's sweeps need, for a shot running on its own sub-grid
@@ -185,9 +186,10 @@ int launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, cons
 template <int K>
 int launch_bwd_C(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err);
-// Adds the per-shot gradients of the first nshots slots into the global ones.
+// Adds the per-shot gradients (when g_lam is not null) and illuminations (when
+// g_illum is not null) of the first nshots slots into the global ones.
 void launch_reduce_grads(cudaStream_t s, int nz, int nx, int ldz, int nshots, const ShotSlot* slots, float* g_lam,
-                         float* g_mu, float* g_den);
+                         float* g_mu, float* g_den, float* g_illum);
 
 // Model set-up: row-major double (lambda, mu in MPa) -> column-major float media.
 // cpmax_bits receives atomicMax of the P velocity's float bits.

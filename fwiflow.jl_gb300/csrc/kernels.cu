@@ -304,8 +304,11 @@ __device__ __forceinline__ void fwd_velocity_edge(const SweepPack<K>& P, int sho
     f.m_dsxx_dx[i] = mm;
     dsxx_dx = dsxx_dx / c.K_xh[x] + mm;
   }
-  f.vz[i] = vz + (dszz_dz + dsxz_dx) * bA * g.dt;
-  f.vx[i] = vx + (dsxz_dz + dsxx_dx) * bB * g.dt;
+  const float nvz = vz + (dszz_dz + dsxz_dx) * bA * g.dt;
+  const float nvx = vx + (dsxz_dz + dsxx_dx) * bB * g.dt;
+  f.vz[i] = nvz;
+  f.vx[i] = nvx;
+  if (S.gr.illum) S.gr.illum[i] += nvz * nvz + nvx * nvx;
 }
 
 // ---------------------------------------------------------------------------
@@ -604,8 +607,11 @@ __device__ __forceinline__ void fwd_velocity_fast(const SweepPack<K>& P, int sho
   const float dsxz_dx = sdm(s_sxz, b, kBoxZ, g.rdx);
   const float dsxz_dz = sdm(s_sxz, b, 1, g.rdz);
   const float dsxx_dx = sdp(s_sxx, b, kBoxZ, g.rdx);
-  f.vz[i] = vz + (dszz_dz + dsxz_dx) * bA * g.dt;
-  f.vx[i] = vx + (dsxz_dz + dsxx_dx) * bB * g.dt;
+  const float nvz = vz + (dszz_dz + dsxz_dx) * bA * g.dt;
+  const float nvx = vx + (dsxz_dz + dsxx_dx) * bB * g.dt;
+  f.vz[i] = nvz;
+  f.vx[i] = nvx;
+  if (S.gr.illum) S.gr.illum[i] += nvz * nvz + nvx * nvx;
 }
 
 template <int TX, int K>
@@ -906,27 +912,38 @@ __global__ void __launch_bounds__(kResThreads)
   }
 }
 
-// Adds the per-shot gradients of a shot group into the global gradients, in
-// group order (deterministic): shot k's sub-grid column j is global padded
-// column x_off[k] + j.
+// Adds the per-shot gradients and / or illuminations of a shot group into
+// the global ones, in group order (deterministic): shot k's sub-grid column j
+// is global padded column x_off[k] + j.
 __global__ void k_reduce_grads(int nz, int nx, int ldz, int nshots, const ShotSlot* __restrict__ slots, float* g_lam,
-                               float* g_mu, float* g_den) {
+                               float* g_mu, float* g_den, float* g_illum) {
   const int z = blockIdx.x * blockDim.x + threadIdx.x;
   const int x = blockIdx.y * blockDim.y + threadIdx.y;
   if (z >= nz || x >= nx) return;
   const size_t i = static_cast<size_t>(x) * ldz + z;
-  float a = g_lam[i], b = g_mu[i], c = g_den[i];
-  for (int k = 0; k < nshots; ++k) {
-    const int xs = x - slots[k].x_off;
-    if (xs < 0 || xs >= slots[k].g.nx) continue;
-    const size_t j = static_cast<size_t>(xs) * ldz + z;
-    a += slots[k].gr.lam[j];
-    b += slots[k].gr.mu[j];
-    c += slots[k].gr.den[j];
+  if (g_lam) {
+    float a = g_lam[i], b = g_mu[i], c = g_den[i];
+    for (int k = 0; k < nshots; ++k) {
+      const int xs = x - slots[k].x_off;
+      if (xs < 0 || xs >= slots[k].g.nx) continue;
+      const size_t j = static_cast<size_t>(xs) * ldz + z;
+      a += slots[k].gr.lam[j];
+      b += slots[k].gr.mu[j];
+      c += slots[k].gr.den[j];
+    }
+    g_lam[i] = a;
+    g_mu[i] = b;
+    g_den[i] = c;
   }
-  g_lam[i] = a;
-  g_mu[i] = b;
-  g_den[i] = c;
+  if (g_illum) {
+    float e = g_illum[i];
+    for (int k = 0; k < nshots; ++k) {
+      const int xs = x - slots[k].x_off;
+      if (xs < 0 || xs >= slots[k].g.nx) continue;
+      e += slots[k].gr.illum[static_cast<size_t>(xs) * ldz + z];
+    }
+    g_illum[i] = e;
+  }
 }
 
 // Fixed-order sum of the block partials into *acc (one warp).
@@ -1088,9 +1105,9 @@ void launch_sum_partials(cudaStream_t s, const double* partials, int n, double* 
 }
 
 void launch_reduce_grads(cudaStream_t s, int nz, int nx, int ldz, int nshots, const ShotSlot* slots, float* g_lam,
-                         float* g_mu, float* g_den) {
+                         float* g_mu, float* g_den, float* g_illum) {
   dim3 grid((nz + 31) / 32, (nx + 7) / 8);
-  k_reduce_grads<<<grid, dim3(32, 8), 0, s>>>(nz, nx, ldz, nshots, slots, g_lam, g_mu, g_den);
+  k_reduce_grads<<<grid, dim3(32, 8), 0, s>>>(nz, nx, ldz, nshots, slots, g_lam, g_mu, g_den, g_illum);
 }
 
 void launch_to_rowmajor(cudaStream_t s, int nz, int nx, int ldz, const float* src, double* dst, double scale) {

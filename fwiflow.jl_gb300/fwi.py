@@ -189,6 +189,17 @@ class FwiContext:
     def last_group_count(self) -> int:
         return int(self._lib.fwigb_last_group_count(self._h))
 
+    def set_illumination(self, enable: bool = True) -> None:
+        """Accumulate the source illumination sum_t (vz^2 + vx^2) in the
+        following runs (all their shots)."""
+        _lib.check(self._lib.fwigb_set_illumination(self._h, int(enable)), self._h)
+
+    def illumination(self) -> np.ndarray:
+        """The last run's illumination, [nz][nx] float64."""
+        out = np.zeros((self.nz, self.nx))
+        _lib.check(self._lib.fwigb_fetch_illumination(self._h, _lib.dptr(out)), self._h)
+        return out
+
     def tile_config(self):
         """Tile widths of (forward stress, forward velocity, backward B, backward C)."""
         t = np.zeros(4, dtype=np.int32)

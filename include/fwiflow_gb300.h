@@ -153,6 +153,15 @@ int fwigb_set_batching(fwigb_ctx *ctx, int max_shots, unsigned long long mem_bud
 /* Number of shot groups the last fwigb_run used. */
 int fwigb_last_group_count(const fwigb_ctx *ctx);
 
+/* Source illumination (no counterpart in the reference): with enable != 0 the
+ * following runs also accumulate, over all their shots and forward steps, the
+ * energy vz^2 + vx^2 of the forward velocity after each step (the diagonal
+ * pseudo-Hessian proxy used to precondition the gradient).
+ * fwigb_fetch_illumination copies the last run's sum as row-major double
+ * [nz][nx]; it fails if that run did not accumulate it. */
+int fwigb_set_illumination(fwigb_ctx *ctx, int enable);
+int fwigb_fetch_illumination(fwigb_ctx *ctx, double *illum);
+
 /* Tile widths (columns per thread block: 4, 8 or 16) of the four sweeps
  * (forward stress, forward velocity, backward B, backward C). By default an
  * autotuner times every width on the context's grid at the first run and keeps
@@ -188,6 +197,46 @@ int fwigb_misfit_gathers_noalloc(const float *d_obs, float *d_syn, float *d_res,
 
 /* Message of the last failure of fwigb_misfit_gathers_noalloc (thread-local). */
 const char *fwigb_noalloc_last_error(void);
+
+/* ---- Learned gradient preconditioner: BF16 tensor-core 3x3 convolutions
+ * (csrc/cnn.cu; no counterpart in the reference). Images are Hz x Wx pixels
+ * (Hz a multiple of 32), x-major with z fastest, channels innermost and
+ * padded to 16 or 32; BF16 activations, FP32 accumulation, weights packed in
+ * tensor-core fragment order by fwigb_cnn_pack_weights. All calls enqueue on
+ * `stream` (a cudaStream_t) and allocate nothing. ---- */
+
+/* y = epilogue(conv3x3(x, W) + b), zero padding. (cin_pad, cout_pad) in
+ * {(16,32), (32,32), (32,16)}. epilogue 0: GELU, writes the pre-activation to
+ * z_pre and GELU of it to y_bf16; 1: linear, y_f32 (FP32); 2: no bias,
+ * y_bf16 = conv(x, W) * GELU'(z_prev) (the data gradient through the previous
+ * layer's GELU, with W packed transposed). */
+int fwigb_cnn_conv3x3(const void *x, int Hz, int Wx, int cin_pad, int cout_pad, int epilogue, const void *wfrag,
+                      const float *bias, void *y_bf16, float *y_f32, void *z_pre, const void *z_prev,
+                      void *stream);
+/* Number of 32 x 8 pixel tiles (blocks) of an Hz x Wx image. */
+int fwigb_cnn_tile_count(int Hz, int Wx);
+/* Per-tile partial weight gradients [tiles][9][cin_pad][cout_pad] (FP32) of
+ * dL/dW[tap][ci][co] = sum_p x(p + tap offset)[ci] dz(p)[co]. */
+int fwigb_cnn_wgrad_partials(const void *x, const void *dz, int Hz, int Wx, int cin_pad, int cout_pad,
+                             float *partials, void *stream);
+/* out[i] = sum over blocks b (in order) of partials[b * n + i]. */
+int fwigb_cnn_reduce_partials(const float *partials, int nblocks, int n, float *out, void *stream);
+/* Per-chunk partial sums over pixels of dz[p][c] (bias gradient):
+ * partials[ceil(npix / chunk)][c_pad]. */
+int fwigb_cnn_bias_partials(const void *dz, long long npix, int c_pad, int chunk, float *partials, void *stream);
+/* Adam step (bias-corrected) on n FP32 parameters; step counts from 1. */
+int fwigb_cnn_adam(float *w, const float *grad, float *m1, float *m2, int n, float lr, float beta1, float beta2,
+                   float eps, int step, void *stream);
+/* Packs FP32 weights W[9][cin][cout] into fragment order for a convolution
+ * with cin_pad inputs / cout_pad outputs, or (transposed != 0) for its data
+ * gradient: W'[tap][co][ci] = W[8 - tap][ci][co]. */
+int fwigb_cnn_pack_weights(const float *w, int cin, int cout, int cin_pad, int cout_pad, int transposed, void *frag,
+                           void *stream);
+/* Masked MSE of the first nc channels of y (FP32 [npix][c_pad]) against
+ * target (FP32 [npix][nc]): per-256-pixel partial loss sums, and
+ * dy = 2 (y - target) mask * inv_count as BF16 [npix][c_pad]. c_pad = 16. */
+int fwigb_cnn_mse_grad(const float *y, const float *target, const float *mask, long long npix, int c_pad, int nc,
+                       float inv_count, void *dy, float *partials, void *stream);
 
 #ifdef __cplusplus
 }

@@ -574,10 +574,11 @@ enum { ORACLE_OK = 0, ORACLE_BAD_ARG = 1, ORACLE_COURANT = 3 };
 // [nrec][nSteps] (calc 0/1). syn_out[i] (optional) receives shot i's gathers as
 // the reference keeps them: raw for calc 2, after the taper for calc 0/1.
 // res_out[i] (optional) receives the adjoint source (tapered residual).
-int oracle_cufd(const oracle_para* p, const oracle_shot* shots, int group_size, const int* shot_ids,
-                const double* Lambda, const double* Mu, const double* Den, const double* stf, int calc_id,
-                const float* const* obs, float* const* syn_out, float* const* res_out, double* misfit,
-                double* grad_Lambda, double* grad_Mu, double* grad_Den, double* grad_stf, int nthreads) {
+static int cufd_impl(const oracle_para* p, const oracle_shot* shots, int group_size, const int* shot_ids,
+                     const double* Lambda, const double* Mu, const double* Den, const double* stf, int calc_id,
+                     const float* const* obs, float* const* syn_out, float* const* res_out, double* misfit,
+                     double* grad_Lambda, double* grad_Mu, double* grad_Den, double* grad_stf, int nthreads,
+                     double* illum) {
   if (calc_id < 0 || calc_id > 2 || !p) return ORACLE_BAD_ARG;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -684,6 +685,12 @@ int oracle_cufd(const oracle_para* p, const oracle_shot* shots, int group_size, 
       stress_forward(g, m, c, f);
       add_source(g, f, src[it], zs, xs, true, gauss);
       velocity_forward(g, m, c, f);
+      if (illum)  // source illumination: sum over forward steps of vz^2 + vx^2 (this package's definition)
+        for (int z = 0; z < nz; ++z)
+          for (int x = 0; x < nx; ++x) {
+            const double a = f.vz[g.at(z, x)], b = f.vx[g.at(z, x)];
+            illum[static_cast<size_t>(z) * nx + x] += a * a + b * b;
+          }
       for (int r = 0; r < nrec; ++r)
         data[static_cast<size_t>(r) * nSteps + it + 1] = static_cast<float>(f.szz[rec[r]] + kRSXXZZ * f.sxx[rec[r]]);
     }
@@ -762,6 +769,25 @@ int oracle_cufd(const oracle_para* p, const oracle_shot* shots, int group_size, 
   }
   if (if_res && !withAdj && misfit) *misfit = 0.5f * l2;  // libCUFD.cu:528-536 (float accumulator)
   return ORACLE_OK;
+}
+
+int oracle_cufd(const oracle_para* p, const oracle_shot* shots, int group_size, const int* shot_ids,
+                const double* Lambda, const double* Mu, const double* Den, const double* stf, int calc_id,
+                const float* const* obs, float* const* syn_out, float* const* res_out, double* misfit,
+                double* grad_Lambda, double* grad_Mu, double* grad_Den, double* grad_stf, int nthreads) {
+  return cufd_impl(p, shots, group_size, shot_ids, Lambda, Mu, Den, stf, calc_id, obs, syn_out, res_out, misfit,
+                   grad_Lambda, grad_Mu, grad_Den, grad_stf, nthreads, nullptr);
+}
+
+// oracle_cufd that also adds the source illumination of every shot, row-major
+// [nz][nx] double, into illum (the caller zeroes it).
+int oracle_cufd_illum(const oracle_para* p, const oracle_shot* shots, int group_size, const int* shot_ids,
+                      const double* Lambda, const double* Mu, const double* Den, const double* stf, int calc_id,
+                      const float* const* obs, float* const* syn_out, float* const* res_out, double* misfit,
+                      double* grad_Lambda, double* grad_Mu, double* grad_Den, double* grad_stf, int nthreads,
+                      double* illum) {
+  return cufd_impl(p, shots, group_size, shot_ids, Lambda, Mu, Den, stf, calc_id, obs, syn_out, res_out, misfit,
+                   grad_Lambda, grad_Mu, grad_Den, grad_stf, nthreads, illum);
 }
 
 }  // extern "C"

@@ -130,7 +130,7 @@ def _iptr(a):
 
 
 def _run_group(p: dict, shots: list, ids: Sequence[int], nz: int, nx: int, nt: int, lam, mu, den, stf, calc_id: int,
-               obs, nthreads: int, precision: str):
+               obs, nthreads: int, precision: str, illum: Optional[np.ndarray] = None):
     """One oracle_cufd call over shots sharing one grid and record length."""
     para = _Para(nz, nx, nt, p["nPml"], p["nPad"], p["dz"], p["dx"], p["dt"], p["f0"], int(p["if_win"]))
     keep = []
@@ -163,10 +163,11 @@ def _run_group(p: dict, shots: list, ids: Sequence[int], nz: int, nx: int, nt: i
     g_den = np.zeros((nz, nx))
     g_stf = np.zeros_like(stf)
     cids = np.asarray(ids, dtype=np.int32)
-    rc = _load_oracle(precision).oracle_cufd(
-        ctypes.byref(para), carr, n, _iptr(cids), _dptr(lam), _dptr(mu), _dptr(den), _dptr(stf), int(calc_id),
-        obs_ptrs, syn_ptrs, None, ctypes.byref(misfit), _dptr(g_lam), _dptr(g_mu), _dptr(g_den), _dptr(g_stf),
-        int(nthreads))
+    lib = _load_oracle(precision)
+    args = (ctypes.byref(para), carr, n, _iptr(cids), _dptr(lam), _dptr(mu), _dptr(den), _dptr(stf), int(calc_id),
+            obs_ptrs, syn_ptrs, None, ctypes.byref(misfit), _dptr(g_lam), _dptr(g_mu), _dptr(g_den), _dptr(g_stf),
+            int(nthreads))
+    rc = lib.oracle_cufd(*args) if illum is None else lib.oracle_cufd_illum(*args, _dptr(illum))
     if rc != 0:
         raise RuntimeError(f"oracle_cufd failed with status {rc}")
     return misfit.value, g_lam, g_mu, g_den, g_stf, [a.reshape(s["nrec"], nt) for a, s in zip(syn, shots)]
@@ -174,7 +175,7 @@ def _run_group(p: dict, shots: list, ids: Sequence[int], nz: int, nx: int, nt: i
 
 def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads: int = 0,
          obs: Optional[Sequence[np.ndarray]] = None, write_files: bool = True, want_gathers: bool = False,
-         precision: str = "reference") -> dict:
+         precision: str = "reference", want_illum: bool = False) -> dict:
     """Oracle run of one `cufd` call (libCUFD.cu:34-580).
 
     lam, mu [MPa] and den are row-major float64 [nz][nx]; stf is
@@ -184,6 +185,8 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
     Returns misfit, g_lambda, g_mu, g_den, g_stf and (optionally) gathers
     (shot k's gather is [nrec][its record length]).
     precision "fp32" runs the FP32-only build (no double promotions).
+    want_illum adds "illum": the source illumination (sum over shots and
+    forward steps of vz^2 + vx^2 after each velocity update), [nz][nx].
     """
     p = load_para(para_fname)
     shot_ids = [int(v) for v in np.asarray(shot_ids).ravel()]
@@ -199,9 +202,10 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
         obs = [np.fromfile(os.path.join(p["data_dir_name"], f"Shot{sid}.bin"), dtype=np.float32,
                            count=s["nrec"] * s.get("nSteps", nt)) for sid, s in zip(shot_ids, shots)]
     extended = any("nSteps" in s or "win_x0" in s for s in shots)
+    illum = np.zeros((nz, nx)) if want_illum else None
     if not extended:
         misfit, g_lam, g_mu, g_den, g_stf, gathers = _run_group(p, shots, shot_ids, nz, nx, nt, lam, mu, den, stf,
-                                                                calc_id, obs, nthreads, precision)
+                                                                calc_id, obs, nthreads, precision, illum)
     else:
         # Each shot alone on its sub-model, for its own record length.
         misfit = 0.0
@@ -220,9 +224,12 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
             nxk = x1 - x0 + 1 + 2 * nPml
             stf_k = np.ascontiguousarray(stf[sid:sid + 1, :ntk])
             ob = None if obs is None else [obs[k]]
+            il = None if illum is None else np.zeros((nz, nxk))
             m, gl, gm, gd, gs, gth = _run_group(p, [sub], [0], nz, nxk, ntk, np.ascontiguousarray(lam[:, cols]),
                                                np.ascontiguousarray(mu[:, cols]), np.ascontiguousarray(den[:, cols]),
-                                               stf_k, calc_id, ob, nthreads, precision)
+                                               stf_k, calc_id, ob, nthreads, precision, il)
+            if il is not None:
+                illum[:, cols] += il
             misfit += m
             g_lam[:, cols] += gl
             g_mu[:, cols] += gm
@@ -230,6 +237,8 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
             g_stf[sid, :ntk] += gs[0]
             gathers += gth
     out = {"misfit": misfit, "g_lambda": g_lam, "g_mu": g_mu, "g_den": g_den, "g_stf": g_stf}
+    if illum is not None:
+        out["illum"] = illum
     if calc_id == 2 and write_files:
         for sid, a in zip(shot_ids, gathers):
             a.astype(np.float32).tofile(os.path.join(p["data_dir_name"], f"Shot{sid}.bin"))

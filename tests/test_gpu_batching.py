@@ -141,3 +141,27 @@ def test_memory_budget_splits_groups(gpu_lib, fw, tmp_path):
     for x, y in zip(a[1:], b[1:]):
         assert rel(x, y) < 1e-6
     ctx.close()
+
+
+def test_illumination_matches_oracle(gpu_lib, fw, orc, tmp_path):
+    """Source illumination sum_t (vz^2 + vx^2) over all shots, windowed and
+    uneven ones included, against the oracle (1e-4 relative L2); it is
+    accumulated in any run (here a misfit-only one) and only when enabled."""
+    w = uneven_tiny(n_shots=4, seed=14, nSteps=200)
+    para = w.write_files(str(tmp_path))
+    ids = list(range(len(w.shots)))
+    _observe(orc, w, para, ids)
+    lam, mu, rho = w.moduli()
+    ref = orc.cufd(0, lam, mu, rho, w.stf, ids, para, want_illum=True)["illum"]
+    ctx = fw.FwiContext(para, 0)
+    ctx.set_illumination(True)
+    J = ctx.misfit(lam, mu, rho, w.stf, ids)
+    assert rel(ctx.illumination(), ref) < TOL_DATA
+    ctx.set_batching(max_shots=1)
+    ctx.misfit_grad(lam, mu, rho, w.stf, ids)
+    assert rel(ctx.illumination(), ref) < TOL_DATA
+    ctx.set_illumination(False)
+    assert ctx.misfit(lam, mu, rho, w.stf, ids) == pytest.approx(J, rel=1e-6)
+    with pytest.raises(fw.FwiError):
+        ctx.illumination()
+    ctx.close()
