@@ -8,7 +8,7 @@ from .utils import (FWIGeometry, default_nPad, padding, paraGen, sourceGene, sur
 from .fwi import (FWI, FwiContext, FwiOpFunction, compute_misfit, compute_observation, fwi_obs_op, fwi_op,
                   fwi_op_grad)
 from ._lib import FwiError, LIB_PATH
-from . import gradcheck, shots, synthetic
+from . import gradcheck, inversion, precond, shots, synthetic
 
 __all__ = [
     "FWI", "FwiContext", "FwiOpFunction", "FwiError", "FWIGeometry", "LIB_PATH", "compute_misfit",

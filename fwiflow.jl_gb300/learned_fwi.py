@@ -1,0 +1,144 @@
+"""Learned-preconditioner FWI experiment: time to a target relative model
+error, learned vs plain, on one GPU.
+
+1. Training set: for each training model of the layered + random-field family
+   (synthetic.layered_grf, seeds train_seed..), the operator computes the
+   observed data of the true model and, at the starting model, the lambda /
+   mu / rho gradients with the source illumination; each gives one (features,
+   pseudo-Hessian target, mask) sample (precond.py).
+2. The CNN trains on those samples with the library's own kernels (Adam).
+3. Held-out models (seeds eval_seed..): inversions from the starting model
+   with plain steepest descent, learned-preconditioned descent (falling back
+   to the plain step when its step does not lower the misfit), the exact
+   pseudo-Hessian descent, and plain L-BFGS; each records misfit, model error
+   and wall time per iteration.
+
+    python fwiflow.jl_gb300/learned_fwi.py [--train-models 64] [--eval-models 4] [--iters 20] [--out FILE]
+
+prints one JSON line (per method: the median over the held-out models of the
+time to the target error and of the final error).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+
+def main(argv=None) -> None:
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import __graft_entry__ as ge
+
+    fw = ge.load_package()
+    from fwiflow_gb300 import inversion, precond, synthetic
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train-models", type=int, default=64)
+    ap.add_argument("--eval-models", type=int, default=4)
+    ap.add_argument("--iters", type=int, default=20)
+    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--target-error", type=float, default=0.01)
+    ap.add_argument("--nz", type=int, default=256)
+    ap.add_argument("--nx", type=int, default=768)
+    ap.add_argument("--shots", type=int, default=16)
+    ap.add_argument("--nsteps", type=int, default=2000)
+    ap.add_argument("--smooth", type=float, default=10.0, help="starting model: true model smoothed (cells)")
+    ap.add_argument("--train-seed", type=int, default=1000)
+    ap.add_argument("--eval-seed", type=int, default=2000)
+    ap.add_argument("--methods", default="plain,learned,pseudo_hessian,lbfgs")
+    ap.add_argument("--out", default=None, help="write the full histories (JSON) here")
+    args = ap.parse_args(argv)
+
+    def log(*a):
+        print(*a, file=sys.stderr, flush=True)
+
+    def model(seed):
+        return synthetic.layered_grf(seed, nz=args.nz, nx=args.nx, n_shots=args.shots, nSteps=args.nsteps,
+                                     smooth_cells=args.smooth)
+
+    w0 = model(args.train_seed)
+    para = w0.write_files(tempfile.mkdtemp())  # geometry shared by the whole family
+    ctx = fw.FwiContext(para, 0)
+    ids = list(range(len(w0.shots)))
+    mask = inversion.inversion_mask(w0.nz_pad, w0.nx_pad, w0.nz, w0.nx, w0.nPml)
+
+    def problem_of(w):
+        obs = ctx.obs(*inversion.moduli_of_vp(w.vp_obs), w.stf, ids, write_files=False)
+        return inversion.VpProblem(ctx, w.stf, ids, obs, w.vp, w.vp_obs, mask)
+
+    def sample_of(prob):
+        _, g, grads, illum = prob.misfit_grad(prob.vp0, illumination=True)
+        return (precond.features(*grads, illum, mask), precond.pseudo_hessian_target(*grads, illum, mask), mask)
+
+    t0 = time.perf_counter()
+    train = [sample_of(problem_of(model(args.train_seed + k))) for k in range(args.train_models)]
+    t_data = time.perf_counter() - t0
+    log(f"training set: {len(train)} samples in {t_data:.1f} s")
+    evals = [model(args.eval_seed + k) for k in range(args.eval_models)]
+    val = [sample_of(problem_of(w)) for w in evals]
+
+    net = precond.CnnPreconditioner(w0.nz_pad, w0.nx_pad, seed=0)
+    t0 = time.perf_counter()
+    loss0 = net.evaluate(val)
+    hist = net.train(train, args.epochs, lr=args.lr)
+    t_train = time.perf_counter() - t0
+    val_loss = net.evaluate(val)
+    log(f"trained {args.epochs} epochs in {t_train:.1f} s: train loss {hist[0]:.4g} -> {hist[-1]:.4g}, "
+        f"held-out loss {loss0:.4g} -> {val_loss:.4g}")
+
+    methods = args.methods.split(",")
+    results = {m: [] for m in methods}
+    for w in evals:
+        for m in methods:
+            prob = problem_of(w)
+            if m == "plain":
+                h = inversion.descent(prob, args.iters)
+            elif m == "learned":
+                h = inversion.descent(prob, args.iters, inversion.learned_preconditioner(net))
+            elif m == "pseudo_hessian":
+                h = inversion.descent(prob, args.iters, inversion.pseudo_hessian_preconditioner())
+            elif m == "lbfgs":
+                h = inversion.lbfgs(prob, args.iters)
+            else:
+                raise ValueError(m)
+            d = h.as_dict()
+            d["time_to_target_s"] = h.time_to_error(args.target_error)
+            d["seed"] = w.extra["seed"]
+            results[m].append(d)
+            log(f"model {w.extra['seed']} {m:15s} error {h.model_error[0]:.4f} -> {h.model_error[-1]:.4f} "
+                f"in {len(h.model_error) - 1} it, {h.wall[-1]:.1f} s, time to {args.target_error:g}: "
+                f"{d['time_to_target_s']}")
+
+    def med(v):
+        v = [x for x in v if x is not None]
+        return float(np.median(v)) if v else None
+
+    summary = {}
+    for m, rs in results.items():
+        tt = [r["time_to_target_s"] for r in rs]
+        summary[m] = {"reached": sum(t is not None for t in tt), "models": len(rs),
+                      "median_time_to_target_s": med(tt),
+                      "median_final_error": med([r["model_error"][-1] for r in rs]),
+                      "median_start_error": med([r["model_error"][0] for r in rs]),
+                      "median_wall_s": med([r["wall_s"][-1] for r in rs])}
+    line = {"experiment": "time to relative model error, learned vs plain preconditioner",
+            "target_error": args.target_error, "grid": [w0.nz_pad, w0.nx_pad], "nSteps": args.nsteps,
+            "shots": args.shots, "train_models": args.train_models, "eval_models": args.eval_models,
+            "iters": args.iters, "training_data_s": t_data, "training_s": t_train, "train_loss": hist,
+            "heldout_loss": [loss0, val_loss], "methods": summary}
+    print(json.dumps(line))
+    if args.out:
+        with open(args.out, "w") as f:
+            json.dump({"summary": line, "histories": results}, f)
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -31,33 +31,41 @@ def _torch():
     return torch
 
 
-def features(g_lambda, g_mu, g_den, illum, mask) -> np.ndarray:
-    """The 5 input channels, each (nz, nx): the three gradients scaled by
-    their RMS inside the mask, the illumination scaled by its maximum, and
-    its log10 (floored at 1e-6 of the maximum), shifted to [0, 1]."""
+def _rms(a, m):
+    s = float(np.sqrt(np.mean(np.square(a[m])))) if m.any() else 0.0
+    return s if s > 0 else 1.0
+
+
+def gradient_scales(g_lambda, g_mu, g_den, mask) -> np.ndarray:
+    """RMS of each raw gradient inside the mask: the per-channel unit of the
+    network's inputs and outputs."""
     m = mask > 0
-    out = []
-    for g in (g_lambda, g_mu, g_den):
-        s = np.sqrt(np.mean(np.square(g[m]))) if m.any() else 1.0
-        out.append(g / (s if s > 0 else 1.0))
+    return np.array([_rms(g, m) for g in (g_lambda, g_mu, g_den)])
+
+
+def features(g_lambda, g_mu, g_den, illum, mask) -> np.ndarray:
+    """The 5 input channels, each (nz, nx): the three gradients in units of
+    their RMS inside the mask, the illumination over its maximum, and its
+    log10 (floored at 1e-6 of the maximum) mapped to [0, 1]."""
+    sc = gradient_scales(g_lambda, g_mu, g_den, mask)
     imax = float(illum.max()) if illum.max() > 0 else 1.0
     e = illum / imax
-    out.append(e)
-    out.append((np.log10(np.maximum(e, 1e-6)) + 6.0) / 6.0)
-    return np.stack(out)
+    return np.stack([g_lambda / sc[0], g_mu / sc[1], g_den / sc[2], e, (np.log10(np.maximum(e, 1e-6)) + 6.0) / 6.0])
 
 
-def pseudo_hessian_target(g_lambda, g_mu, g_den, illum, mask, eps: float = 1e-3) -> np.ndarray:
-    """g / (H_diag + eps * max H_diag) per parameter, each scaled by its RMS
-    inside the mask: the training target (3, nz, nx)."""
-    h = illum + eps * float(illum.max())
-    m = mask > 0
-    out = []
-    for g in (g_lambda, g_mu, g_den):
-        t = g / h
-        s = np.sqrt(np.mean(np.square(t[m]))) if m.any() else 1.0
-        out.append(t / (s if s > 0 else 1.0) * mask)
-    return np.stack(out)
+def illumination_gain(illum, eps: float = 0.05) -> np.ndarray:
+    """The diagonal pseudo-Hessian preconditioner as a gain: 1 / (H / max H + eps)."""
+    imax = float(illum.max()) if illum.max() > 0 else 1.0
+    return 1.0 / (illum / imax + eps)
+
+
+def pseudo_hessian_target(g_lambda, g_mu, g_den, illum, mask, eps: float = 0.05) -> np.ndarray:
+    """Training target (3, nz, nx): g / (H_diag + eps max H_diag) for each
+    parameter, in the units of the input channels (each gradient over its
+    RMS, the gain normalised by max H_diag), zero outside the mask."""
+    sc = gradient_scales(g_lambda, g_mu, g_den, mask)
+    gain = illumination_gain(illum, eps)
+    return np.stack([g / s * gain * mask for g, s in zip((g_lambda, g_mu, g_den), sc)])
 
 
 class CnnPreconditioner:
@@ -240,9 +248,17 @@ class CnnPreconditioner:
         return tot / max(len(samples), 1)
 
     def predict(self, feats: np.ndarray) -> np.ndarray:
-        """Preconditioned update (3, nz, nx) for the features (5, nz, nx)."""
+        """Network output (3, nz, nx) for the features (5, nz, nx), in the
+        units of the input channels."""
         self.stage(feats)
         return self.from_image(self.forward(), N_OUT)
+
+    def precondition(self, g_lambda, g_mu, g_den, illum, mask) -> np.ndarray:
+        """Preconditioned lambda / mu / rho gradients (3, nz, nx) in the
+        gradients' own units: the network output times each gradient's RMS."""
+        sc = gradient_scales(g_lambda, g_mu, g_den, mask)
+        out = self.predict(features(g_lambda, g_mu, g_den, illum, mask))
+        return out * sc[:, None, None] * mask
 
     def state(self) -> dict:
         return {f"W{k}": self.W[k].cpu().numpy() for k in range(DEPTH)} | \

@@ -158,6 +158,41 @@ def batched_uneven(seed: int = 3, nz: int = 512, nx: int = 1536, n_shots: int = 
     return w
 
 
+def layered_grf(seed: int, nz: int = 256, nx: int = 768, n_shots: int = 16, nSteps: int = 2000,
+                dx: float = 10.0, dt: float = 0.001, f0: float = 10.0, smooth_cells: float = 10.0) -> Workload:
+    """One model of the learned-preconditioner family: 5-9 layers (Vp from
+    1500 m/s at the top to 3500-4500 m/s at the bottom, random interface
+    depths and a common dip of up to 5 degrees) times (1 + 3 % GRF, corr. 20
+    cells), seeded. `vp` is the starting model of an inversion (the true
+    model smoothed by a Gaussian of `smooth_cells`), `vp_obs` the true model;
+    n_shots sources evenly spread at depth 2, receivers on every column at
+    depth 2; Ricker f0."""
+    rng = np.random.default_rng(seed)
+    nPml = 32
+    nPad = default_nPad(nz, nPml)
+    nl = int(rng.integers(5, 10))
+    vbot = float(rng.uniform(3500.0, 4500.0))
+    cuts = np.sort(rng.uniform(0.08, 0.95, nl - 1)) * nz
+    vels = np.sort(rng.uniform(1500.0, vbot, nl))
+    vels[0] = 1500.0
+    dip = np.tan(np.deg2rad(rng.uniform(-5.0, 5.0)))
+    zz, xx = np.meshgrid(np.arange(nz), np.arange(nx), indexing="ij")
+    depth = zz - dip * (xx - nx / 2)
+    layer = np.searchsorted(cuts, depth)
+    base = vels[np.clip(layer, 0, nl - 1)]
+    true = base * (1.0 + 0.03 * gaussian_random_field((nz, nx), 20.0, rng))
+    from .gradcheck import smooth
+
+    start = smooth(true, smooth_cells)
+    xs = np.linspace(16, nx - 17, n_shots).astype(int)
+    shots = [{"z_src": 2, "x_src": int(x), "z_rec": [2] * nx, "x_rec": list(range(nx))} for x in xs]
+    stf = np.repeat(sourceGene(f0, nSteps, dt), n_shots, axis=0)
+    w = Workload("layered_grf", nz, nx, nPml, nPad, dx, dx, dt, nSteps, f0, padding(start, nPml, nPad),
+                 padding(true, nPml, nPad), shots, stf)
+    w.extra["seed"] = seed
+    return w
+
+
 def tiny(nz: int = 40, nx: int = 60, nPml: int = 12, nSteps: int = 300, n_shots: int = 2, seed: int = 0,
          cs_zero: bool = False) -> Workload:
     """Small smooth model with a Gaussian anomaly for parity tests (seconds on a CPU)."""
