@@ -111,15 +111,16 @@ class VpProblem:
         return J, chain_to_vp(v, gl, gm, gd) * self.mask, (gl, gm, gd), illum
 
 
-def _line_search(problem: VpProblem, vp, J, d, step_max: float):
-    """Three-point search along -d scaled so that the largest change is
-    step_max m/s: tries a, 2a (or a/2, a/4 when a does not lower J) and the
-    minimum of the parabola through the points. Returns (vp, J, a_used) or
-    None when no point lowers the misfit."""
+def _line_search(problem: VpProblem, vp, J, d, step: float):
+    """Search along -d scaled so that the largest change is `step` m/s:
+    tries a, then 2a if a lowers the misfit (else a/2, a/4, ... five times),
+    and the minimum of the parabola through the best point and its
+    neighbours. Returns (vp, J, largest change in m/s) or None when no point
+    lowers the misfit."""
     dmax = float(np.max(np.abs(d)))
     if dmax == 0.0:
         return None
-    a = step_max / dmax
+    a = step / dmax
     pts = [(0.0, J)]
     Ja = problem.misfit(vp - a * d)
     pts.append((a, Ja))
@@ -127,35 +128,36 @@ def _line_search(problem: VpProblem, vp, J, d, step_max: float):
         J2 = problem.misfit(vp - 2 * a * d)
         pts.append((2 * a, J2))
     else:
-        for k in (0.5, 0.25):
+        k = 0.5
+        for _ in range(5):
             Jk = problem.misfit(vp - k * a * d)
             pts.append((k * a, Jk))
             if Jk < J:
                 break
+            k *= 0.5
     pts.sort()
     best = min(pts, key=lambda p: p[1])
-    if len(pts) >= 3:  # parabola through the best point and its neighbours
-        i = pts.index(best)
-        if 0 < i < len(pts) - 1:
-            (x0, y0), (x1, y1), (x2, y2) = pts[i - 1], pts[i], pts[i + 1]
-            den = (x0 - x1) * (x0 - x2) * (x1 - x2)
-            A = (x2 * (y1 - y0) + x1 * (y0 - y2) + x0 * (y2 - y1)) / den
-            B = (x2 * x2 * (y0 - y1) + x1 * x1 * (y2 - y0) + x0 * x0 * (y1 - y2)) / den
-            if A > 0:
-                xm = -B / (2 * A)
-                if x0 < xm < x2 and abs(xm - x1) > 1e-3 * x1:
-                    Jm = problem.misfit(vp - xm * d)
-                    if Jm < best[1]:
-                        best = (xm, Jm)
+    i = pts.index(best)
+    if 0 < i < len(pts) - 1:  # parabola through the best point and its neighbours
+        (x0, y0), (x1, y1), (x2, y2) = pts[i - 1], pts[i], pts[i + 1]
+        den = (x0 - x1) * (x0 - x2) * (x1 - x2)
+        A = (x2 * (y1 - y0) + x1 * (y0 - y2) + x0 * (y2 - y1)) / den
+        B = (x2 * x2 * (y0 - y1) + x1 * x1 * (y2 - y0) + x0 * x0 * (y1 - y2)) / den
+        if A > 0:
+            xm = -B / (2 * A)
+            if x0 < xm < x2 and abs(xm - x1) > 1e-3 * x1:
+                Jm = problem.misfit(vp - xm * d)
+                if Jm < best[1]:
+                    best = (xm, Jm)
     if best[1] >= J:
         return None
-    return vp - best[0] * d, best[1], best[0]
+    return vp - best[0] * d, best[1], best[0] * dmax
 
 
 def descent(problem: VpProblem, iters: int, precondition: Optional[Callable] = None, step_max: float = 60.0,
             target_error: Optional[float] = None) -> History:
     """Preconditioned steepest descent. precondition(vp, g_vp, grads,
-    illum) -> direction (None: the plain gradient); it gets the
+    illum, mask) -> direction (None: the plain gradient); it gets the
     illumination, which is then accumulated during the gradient runs."""
     h = History()
     vp = problem.vp0.copy()
@@ -165,6 +167,7 @@ def descent(problem: VpProblem, iters: int, precondition: Optional[Callable] = N
     h.wall.append(0.0)
     h.evals.append(0)
     h.fallback.append(False)
+    step = step_max  # trial largest change (m/s); follows the last accepted one
     for _ in range(iters):
         J, g, grads, illum = problem.misfit_grad(vp, illumination=precondition is not None)
         if not h.misfit:
@@ -172,15 +175,16 @@ def descent(problem: VpProblem, iters: int, precondition: Optional[Callable] = N
         used_fallback = False
         res = None
         if precondition is not None:
-            d = precondition(problem.full(vp), g, grads, illum) * problem.mask
+            d = precondition(problem.full(vp), g, grads, illum, problem.mask) * problem.mask
             if np.sum(d * g) > 0:  # a descent direction
-                res = _line_search(problem, vp, J, d, step_max)
+                res = _line_search(problem, vp, J, d, step)
         if res is None:
             used_fallback = precondition is not None
-            res = _line_search(problem, vp, J, g, step_max)
+            res = _line_search(problem, vp, J, g, step)
         if res is None:
             break
-        vp, J, a = res
+        vp, J, change = res
+        step = min(step_max, 1.5 * change)
         vp = np.clip(vp, problem.vmin, problem.vmax)
         h.misfit.append(J)
         h.model_error.append(problem.model_error(vp))
@@ -206,6 +210,7 @@ def lbfgs(problem: VpProblem, iters: int, memory: int = 5, step_max: float = 60.
     h.evals.append(0)
     h.fallback.append(False)
     S, Y = [], []
+    step = step_max
     J, g, _, _ = problem.misfit_grad(vp)
     h.misfit.append(J)
     for _ in range(iters):
@@ -221,16 +226,17 @@ def lbfgs(problem: VpProblem, iters: int, memory: int = 5, step_max: float = 60.
             b = np.sum(y * q) / np.sum(y * s)
             q += (a - b) * s
         d = q * problem.mask
-        res = _line_search(problem, vp, J, d, step_max) if np.sum(d * g) > 0 else None
+        res = _line_search(problem, vp, J, d, step) if np.sum(d * g) > 0 else None
         fell_back = False
         if res is None:
             S.clear()
             Y.clear()
             fell_back = True
-            res = _line_search(problem, vp, J, g, step_max)
+            res = _line_search(problem, vp, J, g, step)
             if res is None:
                 break
-        vp_new, _, _ = res
+        vp_new, _, change = res
+        step = min(step_max, 1.5 * change)
         vp_new = np.clip(vp_new, problem.vmin, problem.vmax)
         J_new, g_new, _, _ = problem.misfit_grad(vp_new)
         s, y = vp_new - vp, g_new - g
@@ -252,13 +258,13 @@ def lbfgs(problem: VpProblem, iters: int, memory: int = 5, step_max: float = 60.
     return h
 
 
-def pseudo_hessian_preconditioner(eps: float = 0.05) -> Callable:
-    """d = g_vp / (H / max H + eps): the exact diagonal preconditioner the
+def pseudo_hessian_preconditioner(eps: Optional[float] = None) -> Callable:
+    """d = g_vp / (H + eps max_mask H): the exact diagonal preconditioner the
     network stands in for."""
-    from .precond import illumination_gain
+    from .precond import EPS, illumination_gain
 
-    def apply(vp, g_vp, grads, illum):
-        return g_vp * illumination_gain(illum, eps)
+    def apply(vp, g_vp, grads, illum, mask):
+        return g_vp * illumination_gain(illum, mask, EPS if eps is None else eps)
 
     return apply
 
@@ -266,8 +272,7 @@ def pseudo_hessian_preconditioner(eps: float = 0.05) -> Callable:
 def learned_preconditioner(net) -> Callable:
     """d = dVp of the network's preconditioned lambda / mu / rho gradients."""
 
-    def apply(vp, g_vp, grads, illum):
-        mask = (g_vp != 0).astype(np.float64)
+    def apply(vp, g_vp, grads, illum, mask):
         pl, pm, pd = net.precondition(*grads, illum, mask)
         return chain_to_vp(vp, pl, pm, pd)
 

@@ -49,7 +49,7 @@ def main(argv=None) -> None:
     ap.add_argument("--nx", type=int, default=768)
     ap.add_argument("--shots", type=int, default=16)
     ap.add_argument("--nsteps", type=int, default=2000)
-    ap.add_argument("--smooth", type=float, default=10.0, help="starting model: true model smoothed (cells)")
+    ap.add_argument("--smooth", type=float, default=4.0, help="starting model: true model smoothed (cells)")
     ap.add_argument("--train-seed", type=int, default=1000)
     ap.add_argument("--eval-seed", type=int, default=2000)
     ap.add_argument("--methods", default="plain,learned,pseudo_hessian,lbfgs")
@@ -94,8 +94,11 @@ def main(argv=None) -> None:
         f"held-out loss {loss0:.4g} -> {val_loss:.4g}")
 
     methods = args.methods.split(",")
+    if "plain" in methods:  # plain first: its final error is the reference level
+        methods = ["plain"] + [m for m in methods if m != "plain"]
     results = {m: [] for m in methods}
     for w in evals:
+        ref_err = None
         for m in methods:
             prob = problem_of(w)
             if m == "plain":
@@ -110,11 +113,15 @@ def main(argv=None) -> None:
                 raise ValueError(m)
             d = h.as_dict()
             d["time_to_target_s"] = h.time_to_error(args.target_error)
+            if m == "plain":
+                ref_err = h.model_error[-1]
+            d["plain_final_error"] = ref_err
+            d["time_to_plain_final_s"] = h.time_to_error(ref_err) if ref_err is not None else None
             d["seed"] = w.extra["seed"]
             results[m].append(d)
-            log(f"model {w.extra['seed']} {m:15s} error {h.model_error[0]:.4f} -> {h.model_error[-1]:.4f} "
+            log(f"model {w.extra['seed']} {m:15s} error {h.model_error[0]:.5f} -> {h.model_error[-1]:.5f} "
                 f"in {len(h.model_error) - 1} it, {h.wall[-1]:.1f} s, time to {args.target_error:g}: "
-                f"{d['time_to_target_s']}")
+                f"{d['time_to_target_s']}, to plain's final error: {d['time_to_plain_final_s']}")
 
     def med(v):
         v = [x for x in v if x is not None]
@@ -125,6 +132,8 @@ def main(argv=None) -> None:
         tt = [r["time_to_target_s"] for r in rs]
         summary[m] = {"reached": sum(t is not None for t in tt), "models": len(rs),
                       "median_time_to_target_s": med(tt),
+                      "median_time_to_plain_final_error_s": med([r["time_to_plain_final_s"] for r in rs]),
+                      "median_final_misfit_ratio": med([r["misfit"][-1] / r["misfit"][0] for r in rs]),
                       "median_final_error": med([r["model_error"][-1] for r in rs]),
                       "median_start_error": med([r["model_error"][0] for r in rs]),
                       "median_wall_s": med([r["wall_s"][-1] for r in rs])}

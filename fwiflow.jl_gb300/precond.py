@@ -43,29 +43,41 @@ def gradient_scales(g_lambda, g_mu, g_den, mask) -> np.ndarray:
     return np.array([_rms(g, m) for g in (g_lambda, g_mu, g_den)])
 
 
+EPS = 1e-3  # damping of the pseudo-Hessian, relative to its maximum inside the mask
+
+
+def normalized_illumination(illum, mask) -> np.ndarray:
+    """Illumination over its maximum inside the mask, clipped to [0, 1] (the
+    cells next to the sources, outside the mask, are far brighter)."""
+    m = mask > 0
+    imax = float(illum[m].max()) if m.any() and illum[m].max() > 0 else 1.0
+    return np.clip(illum / imax, 0.0, 1.0)
+
+
 def features(g_lambda, g_mu, g_den, illum, mask) -> np.ndarray:
     """The 5 input channels, each (nz, nx): the three gradients in units of
-    their RMS inside the mask, the illumination over its maximum, and its
-    log10 (floored at 1e-6 of the maximum) mapped to [0, 1]."""
+    their RMS inside the mask, the normalised illumination, and its log10
+    (floored at 1e-6) mapped to [0, 1]."""
     sc = gradient_scales(g_lambda, g_mu, g_den, mask)
-    imax = float(illum.max()) if illum.max() > 0 else 1.0
-    e = illum / imax
+    e = normalized_illumination(illum, mask)
     return np.stack([g_lambda / sc[0], g_mu / sc[1], g_den / sc[2], e, (np.log10(np.maximum(e, 1e-6)) + 6.0) / 6.0])
 
 
-def illumination_gain(illum, eps: float = 0.05) -> np.ndarray:
-    """The diagonal pseudo-Hessian preconditioner as a gain: 1 / (H / max H + eps)."""
-    imax = float(illum.max()) if illum.max() > 0 else 1.0
-    return 1.0 / (illum / imax + eps)
+def illumination_gain(illum, mask, eps: float = EPS) -> np.ndarray:
+    """The diagonal pseudo-Hessian preconditioner as a gain, in units of its
+    value at the brightest masked cell: eps_n / (H_n + eps_n) with H_n the
+    normalised illumination (so the gain is at most 1)."""
+    return eps / (normalized_illumination(illum, mask) + eps)
 
 
-def pseudo_hessian_target(g_lambda, g_mu, g_den, illum, mask, eps: float = 0.05) -> np.ndarray:
+def pseudo_hessian_target(g_lambda, g_mu, g_den, illum, mask, eps: float = EPS) -> np.ndarray:
     """Training target (3, nz, nx): g / (H_diag + eps max H_diag) for each
     parameter, in the units of the input channels (each gradient over its
-    RMS, the gain normalised by max H_diag), zero outside the mask."""
+    RMS, the gain scaled to at most 1), zero outside the mask."""
     sc = gradient_scales(g_lambda, g_mu, g_den, mask)
-    gain = illumination_gain(illum, eps)
-    return np.stack([g / s * gain * mask for g, s in zip((g_lambda, g_mu, g_den), sc)])
+    gain = illumination_gain(illum, mask, eps)
+    t = np.stack([g / s * gain * mask for g, s in zip((g_lambda, g_mu, g_den), sc)])
+    return t / _rms(t, np.broadcast_to(mask > 0, t.shape))
 
 
 class CnnPreconditioner:
@@ -255,7 +267,8 @@ class CnnPreconditioner:
 
     def precondition(self, g_lambda, g_mu, g_den, illum, mask) -> np.ndarray:
         """Preconditioned lambda / mu / rho gradients (3, nz, nx) in the
-        gradients' own units: the network output times each gradient's RMS."""
+        gradients' own units (to a common factor, which a line search
+        absorbs): the network output times each gradient's RMS."""
         sc = gradient_scales(g_lambda, g_mu, g_den, mask)
         out = self.predict(features(g_lambda, g_mu, g_den, illum, mask))
         return out * sc[:, None, None] * mask

@@ -159,14 +159,16 @@ def batched_uneven(seed: int = 3, nz: int = 512, nx: int = 1536, n_shots: int = 
 
 
 def layered_grf(seed: int, nz: int = 256, nx: int = 768, n_shots: int = 16, nSteps: int = 2000,
-                dx: float = 10.0, dt: float = 0.001, f0: float = 10.0, smooth_cells: float = 10.0) -> Workload:
+                dx: float = 10.0, dt: float = 0.001, f0: float = 10.0, smooth_cells: float = 10.0,
+                start: str = "smooth") -> Workload:
     """One model of the learned-preconditioner family: 5-9 layers (Vp from
     1500 m/s at the top to 3500-4500 m/s at the bottom, random interface
     depths and a common dip of up to 5 degrees) times (1 + 3 % GRF, corr. 20
-    cells), seeded. `vp` is the starting model of an inversion (the true
-    model smoothed by a Gaussian of `smooth_cells`), `vp_obs` the true model;
-    n_shots sources evenly spread at depth 2, receivers on every column at
-    depth 2; Ricker f0."""
+    cells), seeded. `vp_obs` is the true model and `vp` the starting model of
+    an inversion: the true model smoothed by a Gaussian of `smooth_cells`
+    (start "smooth"), or the layers without the random field smoothed by it
+    (start "background"). n_shots sources evenly spread at depth 2, receivers
+    on every column at depth 2; Ricker f0."""
     rng = np.random.default_rng(seed)
     nPml = 32
     nPad = default_nPad(nz, nPml)
@@ -183,11 +185,16 @@ def layered_grf(seed: int, nz: int = 256, nx: int = 768, n_shots: int = 16, nSte
     true = base * (1.0 + 0.03 * gaussian_random_field((nz, nx), 20.0, rng))
     from .gradcheck import smooth
 
-    start = smooth(true, smooth_cells)
+    if start == "smooth":
+        vp0 = smooth(true, smooth_cells)
+    elif start == "background":
+        vp0 = smooth(base, smooth_cells)
+    else:
+        raise ValueError(start)
     xs = np.linspace(16, nx - 17, n_shots).astype(int)
     shots = [{"z_src": 2, "x_src": int(x), "z_rec": [2] * nx, "x_rec": list(range(nx))} for x in xs]
     stf = np.repeat(sourceGene(f0, nSteps, dt), n_shots, axis=0)
-    w = Workload("layered_grf", nz, nx, nPml, nPad, dx, dx, dt, nSteps, f0, padding(start, nPml, nPad),
+    w = Workload("layered_grf", nz, nx, nPml, nPad, dx, dx, dt, nSteps, f0, padding(vp0, nPml, nPad),
                  padding(true, nPml, nPad), shots, stf)
     w.extra["seed"] = seed
     return w
