@@ -3,7 +3,14 @@ that maps the raw lambda / mu / rho gradients and the source illumination of
 an FWI iteration to a preconditioned update. It stands in for the diagonal
 pseudo-Hessian preconditioner g / (H_diag + eps), with H_diag the source
 illumination sum_t (vz^2 + vx^2), and is trained on (gradient,
-illumination) -> g / (H_diag + eps) pairs generated by the operator itself.
+illumination) pairs generated by the operator itself.
+
+Output head: the network's 3 output channels are log-gains, one per
+parameter, and the preconditioned update is g_c * exp(out_c). The training
+target is the log of the pseudo-Hessian gain eps / (H_n + eps) (H_n the
+illumination over its maximum in the mask), so the loss weighs the relative
+gain error of a dark deep cell like that of a bright shallow one; regressing
+g * gain directly lets the bright cells dominate.
 
 Every arithmetic step of the network runs in the library's own sm_103a
 kernels (csrc/cnn.cu: BF16 tensor-core convolutions with FP32 accumulation,
@@ -71,13 +78,11 @@ def illumination_gain(illum, mask, eps: float = EPS) -> np.ndarray:
 
 
 def pseudo_hessian_target(g_lambda, g_mu, g_den, illum, mask, eps: float = EPS) -> np.ndarray:
-    """Training target (3, nz, nx): g / (H_diag + eps max H_diag) for each
-    parameter, in the units of the input channels (each gradient over its
-    RMS, the gain scaled to at most 1), zero outside the mask."""
-    sc = gradient_scales(g_lambda, g_mu, g_den, mask)
-    gain = illumination_gain(illum, mask, eps)
-    t = np.stack([g / s * gain * mask for g, s in zip((g_lambda, g_mu, g_den), sc)])
-    return t / _rms(t, np.broadcast_to(mask > 0, t.shape))
+    """Training target (3, nz, nx): the log of the pseudo-Hessian gain for
+    each parameter (the update is then g_c * exp(target_c) = g_c / (H_diag +
+    eps max H_diag) up to a constant), zero outside the mask."""
+    lg = np.log(illumination_gain(illum, mask, eps)) * mask
+    return np.stack([lg, lg, lg])
 
 
 class CnnPreconditioner:
@@ -266,12 +271,11 @@ class CnnPreconditioner:
         return self.from_image(self.forward(), N_OUT)
 
     def precondition(self, g_lambda, g_mu, g_den, illum, mask) -> np.ndarray:
-        """Preconditioned lambda / mu / rho gradients (3, nz, nx) in the
-        gradients' own units (to a common factor, which a line search
-        absorbs): the network output times each gradient's RMS."""
-        sc = gradient_scales(g_lambda, g_mu, g_den, mask)
+        """Preconditioned lambda / mu / rho gradients (3, nz, nx): each
+        gradient times exp of its predicted log-gain, zero outside the mask."""
         out = self.predict(features(g_lambda, g_mu, g_den, illum, mask))
-        return out * sc[:, None, None] * mask
+        gain = np.exp(np.clip(out, -30.0, 5.0))
+        return np.stack([g_lambda, g_mu, g_den]) * gain * mask
 
     def state(self) -> dict:
         return {f"W{k}": self.W[k].cpu().numpy() for k in range(DEPTH)} | \
