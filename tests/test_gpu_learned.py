@@ -4,7 +4,11 @@ CNN kernels, and what the trained network gains over the method without it
 on a held-out model of the same family:
 
 * its update points where the diagonal pseudo-Hessian preconditioner points
-  (cosine > 0.9 over the mask), far closer than the plain gradient does;
+  (cosine > 0.9 over the mask) and, what preconditioning is for, balances
+  deep against shallow updates like it: the ratio of update norms over the
+  lower and upper halves of the mask is within a factor 1.5 of the exact
+  preconditioner's, and at least twice as close (in log) as the plain
+  gradient's;
 * four descent iterations with it lower the misfit more than four plain
   gradient iterations (each with the same line search; the plain step is the
   learned step's fallback).
@@ -50,7 +54,16 @@ def test_learned_preconditioner_gains_over_plain(gpu_lib, fw, tmp_path):
     learned = inversion.learned_preconditioner(net)(p.full(p.vp0), g, grads, illum, mask) * mask
     c_learned, c_plain = _cos(learned, exact), _cos(g, exact)
     assert c_learned > 0.9, (c_learned, c_plain)
-    assert c_learned > c_plain + 0.1, (c_learned, c_plain)
+    rows = np.nonzero(mask.any(axis=1))[0]
+    mid = (rows[0] + rows[-1] + 1) // 2
+
+    def balance(d):
+        return np.linalg.norm(d[mid:]) / np.linalg.norm(d[:mid])
+
+    e_learned = abs(np.log(balance(learned) / balance(exact)))
+    e_plain = abs(np.log(balance(g) / balance(exact)))
+    assert e_learned < np.log(1.5), (e_learned, e_plain)
+    assert e_learned < 0.5 * e_plain, (e_learned, e_plain)
 
     h_plain = inversion.descent(problem(held), 4)
     h_learned = inversion.descent(problem(held), 4, inversion.learned_preconditioner(net))
