@@ -168,9 +168,10 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def run_cpu_oracle(w, n_steps_sample, reps=1):
-    """Times the oracle (reference algorithm on the host cores) on the first
-    n_steps_sample time steps of the workload; returns (Gpts/s, seconds, threads)."""
+def cpu_oracle_case(w, n_steps_sample):
+    """The CPU sample of the workload: its first n_steps_sample time steps
+    (and, for windowed shots, its first shot), with the observed data of the
+    sample computed once by the oracle. Returns (workload, para, obs)."""
     orc = ge.load_oracle()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
     from dataclasses import replace
@@ -183,14 +184,24 @@ def run_cpu_oracle(w, n_steps_sample, reps=1):
     tmp = tempfile.mkdtemp()
     para = ws.write_files(tmp)
     ids = list(range(len(ws.shots)))
+    obs = orc.cufd(2, *ws.moduli(ws.vp_obs), ws.stf, ids, para, nthreads=cpu_threads(), write_files=False,
+                   want_gathers=True)["gathers"]
+    return ws, para, obs
+
+
+def run_cpu_oracle(case, reps=1):
+    """Times the oracle (reference algorithm on all host cores) on a sample
+    from cpu_oracle_case: misfit + gradient. Returns (Gpts/s, seconds, threads)."""
+    ws, para, obs = case
+    orc = ge.load_oracle()
+    ids = list(range(len(ws.shots)))
     nthreads = cpu_threads()
-    orc.cufd(2, *ws.moduli(ws.vp_obs), ws.stf, ids, para, nthreads=nthreads)  # observed data, untimed
     lam, mu, rho = ws.moduli()
     times = []
     for _ in range(reps):
         t0 = time.perf_counter()
-        orc.cufd(1, lam, mu, rho, ws.stf, ids, para, nthreads=nthreads)
-        orc.cufd(0, lam, mu, rho, ws.stf, ids, para, nthreads=nthreads)
+        orc.cufd(1, lam, mu, rho, ws.stf, ids, para, nthreads=nthreads, obs=obs)
+        orc.cufd(0, lam, mu, rho, ws.stf, ids, para, nthreads=nthreads, obs=obs)
         times.append(time.perf_counter() - t0)
     pts = sum(c * n for c, n in shot_sizes(ws))
     return pts / min(times) / 1e9, times, nthreads
@@ -228,12 +239,13 @@ def main():
         if rank != 0:
             return
         n_sample = max(20, min(args.cpu_sample_steps, w.nSteps) // 2)
+        case = cpu_oracle_case(w, n_sample)
         vals = []
         for _ in range(args.warmup):
-            run_cpu_oracle(w, n_sample)
+            run_cpu_oracle(case)
         t_all = []
         for _ in range(args.steps):
-            g, t, threads = run_cpu_oracle(w, n_sample)
+            g, t, threads = run_cpu_oracle(case)
             vals.append(g)
             t_all += t
         value = statistics.median(vals)
@@ -410,7 +422,7 @@ def main():
     if single:
         line["one_shot_per_launch"] = single
     if not args.no_cpu_baseline:
-        g, t, threads = run_cpu_oracle(w, min(args.cpu_sample_steps, w.nSteps))
+        g, t, threads = run_cpu_oracle(cpu_oracle_case(w, min(args.cpu_sample_steps, w.nSteps)))
         line["cpu_baseline"] = {"value": g, "unit": unit, "cores": threads, "kind": "port",
                                 "sample": f"first {min(args.cpu_sample_steps, w.nSteps)} of {w.nSteps} time steps, "
                                           f"same grid and shots, misfit + gradient, {t[0]:.1f} s"}
