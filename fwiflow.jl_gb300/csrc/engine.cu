@@ -407,10 +407,10 @@ struct fwigb_ctx {
   DevBuf g_fields, g_store, g_grads, g_slots;
   int group_cap = 0;
   // Launch parameter packs of the current group: for a lone shot one
-  // SweepPack<1> per (sweep, tile width); else one SweepPack<kPackShots> per
-  // (sweep, tile width, pack of consecutive members), index
-  // (sweep * 3 + tile slot) * npacks + pack. pack_nx[q] is the widest member
-  // sub-grid of pack q.
+  // SweepPack<1> per (sweep variant, tile width); else one
+  // SweepPack<kPackShots> per (sweep variant, tile width, pack of consecutive
+  // members), index (variant * 3 + tile slot) * npacks + pack. pack_nx[q] is
+  // the widest member sub-grid of pack q.
   int group_size = 0, npacks = 0;
   std::vector<SweepPack<1>> pack1;
   std::vector<SweepPack<kPackShots>> packs;
@@ -423,7 +423,8 @@ struct fwigb_ctx {
   bool model_set = false;
   int last_calc = -1;
   long long launches = 0;
-  int tx[4] = {8, 8, 8, 8};  // tile width per sweep (F1, F2, B, C)
+  int tx[4] = {8, 8, 8, 8};    // tile width per sweep (F1, F2, B, C)
+  int rows[4] = {2, 2, 1, 1};  // depths per thread per sweep (forward: 1 or 2)
   bool tuned_fwd = false, tuned_bwd = false;
   bool autotune = true;
   // per-kernel event timing
@@ -853,17 +854,18 @@ int plan_groups(fwigb_ctx* ctx, bool adj, std::vector<std::vector<int>>& groups)
   return FWIGB_OK;
 }
 
-// Launches sweep `w` (0 F1, 1 F2, 2 B, 3 C) over the first `a` members of
-// the current group at tile width tx, one launch per parameter pack; `arg`
-// is the step (F1) or the backward iteration (B, C). Returns the number of
-// launches.
-int launch_sweep(fwigb_ctx* ctx, int w, int tx, int a, int arg, bool save, unsigned* d_err) {
+// Launches sweep `w` (0 F1, 1 F2, 2 B, 3 C) with `rows` depths per thread
+// (forward sweeps: 1 or 2) over the first `a` members of the current group at
+// tile width tx, one launch per parameter pack; `arg` is the step (F1) or the
+// backward iteration (B, C). Returns the number of launches.
+int launch_sweep(fwigb_ctx* ctx, int w, int tx, int rows, int a, int arg, bool save, unsigned* d_err) {
   cudaStream_t s = ctx->stream;
-  const size_t base = static_cast<size_t>(w * 3 + tx_slot(tx));
+  const int variant = (w < 2 && rows == 2) ? w + 4 : w;
+  const size_t base = static_cast<size_t>(variant * 3 + tx_slot(tx));
   auto go = [&](const auto& pk, int n, const SweepGrid& gr) {
     switch (w) {
-      case 0: return launch_fwd_stress(s, tx, pk, n, gr, arg, save, d_err);
-      case 1: return launch_fwd_velocity(s, tx, pk, n, gr, d_err);
+      case 0: return launch_fwd_stress(s, tx, rows, pk, n, gr, arg, save, d_err);
+      case 1: return launch_fwd_velocity(s, tx, rows, pk, n, gr, d_err);
       case 2: return launch_bwd_B(s, tx, pk, n, gr, arg, d_err);
       default: return launch_bwd_C(s, tx, pk, n, gr, arg, d_err);
     }
@@ -881,7 +883,7 @@ int launch_sweep(fwigb_ctx* ctx, int w, int tx, int a, int arg, bool save, unsig
 int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
   const size_t ldz = ctx->geo.ldz;
   std::vector<ShotSlot> slots(members.size());
-  std::vector<TileMaps> maps(static_cast<size_t>(4 * 3) * ctx->group_cap);
+  std::vector<TileMaps> maps(static_cast<size_t>(kSweepVariants * 3) * ctx->group_cap);
   const int nrm = 0;
   (void)nrm;
   nx_max = 0;
@@ -935,8 +937,9 @@ int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
         ctx->err = why;
         return FWIGB_ERR_CUDA;
       }
-      const TileMaps* per_sweep[4] = {&sm.f1, &sm.f2, &sm.b, &sm.c};
-      for (int w = 0; w < 4; ++w) maps[static_cast<size_t>(w * 3 + t) * ctx->group_cap + k] = *per_sweep[w];
+      const TileMaps* per_sweep[kSweepVariants] = {&sm.f1, &sm.f2, &sm.b, &sm.c, &sm.f1w, &sm.f2w};
+      for (int w = 0; w < kSweepVariants; ++w)
+        maps[static_cast<size_t>(w * 3 + t) * ctx->group_cap + k] = *per_sweep[w];
     }
   }
   // Parameter packs (host; passed by value at every launch).
@@ -948,14 +951,14 @@ int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
   ctx->pack_grid.assign(ctx->npacks, SweepGrid{ctx->p.nz, 0});
   for (int q = 0; q < ctx->npacks; ++q) ctx->pack_grid[q].nx = ctx->pack_nx[q];
   if (G == 1) {
-    ctx->pack1.assign(12, SweepPack<1>{});
-    for (int w = 0; w < 12; ++w) {
+    ctx->pack1.assign(kSweepVariants * 3, SweepPack<1>{});
+    for (int w = 0; w < kSweepVariants * 3; ++w) {
       ctx->pack1[w].maps[0] = maps[static_cast<size_t>(w) * ctx->group_cap];
       ctx->pack1[w].slots[0] = slots[0];
     }
   } else {
-    ctx->packs.assign(static_cast<size_t>(12) * ctx->npacks, SweepPack<kPackShots>{});
-    for (int w = 0; w < 12; ++w)
+    ctx->packs.assign(static_cast<size_t>(kSweepVariants * 3) * ctx->npacks, SweepPack<kPackShots>{});
+    for (int w = 0; w < kSweepVariants * 3; ++w)
       for (int k = 0; k < G; ++k) {
         SweepPack<kPackShots>& pk = ctx->packs[static_cast<size_t>(w) * ctx->npacks + k / kPackShots];
         pk.maps[k % kPackShots] = maps[static_cast<size_t>(w) * ctx->group_cap + k];
@@ -969,39 +972,52 @@ int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
   return FWIGB_OK;
 }
 
-// Tile-width autotuner: times every width of each sweep on the first group of
-// the first run (on its live buffers, which the run then resets) and keeps
-// the fastest. The widths are timed interleaved over several rounds and each
-// keeps its best time, so a transient on the GPU does not decide the choice.
-// The backward sweeps are tuned on the first run with the adjoint.
+// Tile autotuner: times every candidate tile of each sweep on the first
+// group of the first run (on its live buffers, which the run then resets) and
+// keeps the fastest: widths 4, 8, 16 for every sweep, times 1 or 2 depths per
+// thread for the forward sweeps. The candidates are timed interleaved over
+// several rounds and each keeps its best time, so a transient on the GPU does
+// not decide the choice. The backward sweeps are tuned on the first run with
+// the adjoint.
 int autotune(fwigb_ctx* ctx, int nshots, int nx_max, bool adj) {
   cudaStream_t s = ctx->stream;
   unsigned* d_err = reinterpret_cast<unsigned*>(ctx->scal.as<char>() + 16);
   (void)nx_max;
-  constexpr int kRounds = 4, kReps = 5;
-  std::vector<cudaEvent_t> ev(2 * kRounds * 3);
+  constexpr int kRounds = 4, kReps = 5, kMaxCand = 6;
+  std::vector<cudaEvent_t> ev(2 * kRounds * kMaxCand);
   for (cudaEvent_t& e : ev) CK(cudaEventCreate(&e));
   const int kinds_end = (adj && ctx->nSteps_max >= 2) ? 4 : 2;
   for (int kind = ctx->tuned_fwd ? 2 : 0; kind < kinds_end; ++kind) {
-    for (int slot = 0; slot < 3; ++slot) launch_sweep(ctx, kind, kTileXs[slot], nshots, 0, false, d_err);  // warm-up
+    const int ncand = kind < 2 ? 6 : 3;  // (width, rows) candidates
+    auto cand = [&](int q, int& tx, int& rows) {
+      tx = kTileXs[q % 3];
+      rows = q < 3 ? 1 : 2;
+    };
+    for (int q = 0; q < ncand; ++q) {  // warm-up
+      int tx, rows;
+      cand(q, tx, rows);
+      launch_sweep(ctx, kind, tx, rows, nshots, 0, false, d_err);
+    }
     for (int r = 0; r < kRounds; ++r)
-      for (int slot = 0; slot < 3; ++slot) {
-        CK(cudaEventRecord(ev[2 * (r * 3 + slot)], s));
-        for (int k = 0; k < kReps; ++k) launch_sweep(ctx, kind, kTileXs[slot], nshots, 0, false, d_err);
-        CK(cudaEventRecord(ev[2 * (r * 3 + slot) + 1], s));
+      for (int q = 0; q < ncand; ++q) {
+        int tx, rows;
+        cand(q, tx, rows);
+        CK(cudaEventRecord(ev[2 * (r * kMaxCand + q)], s));
+        for (int k = 0; k < kReps; ++k) launch_sweep(ctx, kind, tx, rows, nshots, 0, false, d_err);
+        CK(cudaEventRecord(ev[2 * (r * kMaxCand + q) + 1], s));
       }
     CK(cudaStreamSynchronize(s));
     float best = 1e30f;
-    for (int slot = 0; slot < 3; ++slot) {
+    for (int q = 0; q < ncand; ++q) {
       float t = 1e30f;
       for (int r = 0; r < kRounds; ++r) {
         float ms = 0.0f;
-        CK(cudaEventElapsedTime(&ms, ev[2 * (r * 3 + slot)], ev[2 * (r * 3 + slot) + 1]));
+        CK(cudaEventElapsedTime(&ms, ev[2 * (r * kMaxCand + q)], ev[2 * (r * kMaxCand + q) + 1]));
         t = std::min(t, ms);
       }
       if (t < best) {
         best = t;
-        ctx->tx[kind] = kTileXs[slot];
+        cand(q, ctx->tx[kind], ctx->rows[kind]);
       }
     }
   }
@@ -1091,8 +1107,8 @@ int run(fwigb_ctx* ctx, int calc_id) {
     const int ntop = nst[0];
     for (int it = 0; it <= ntop - 2; ++it) {
       const int a = active(it);
-      TIMED(0, launches += launch_sweep(ctx, 0, ctx->tx[0], a, it, adj, d_err));
-      TIMED(1, launches += launch_sweep(ctx, 1, ctx->tx[1], a, 0, false, d_err));
+      TIMED(0, launches += launch_sweep(ctx, 0, ctx->tx[0], ctx->rows[0], a, it, adj, d_err));
+      TIMED(1, launches += launch_sweep(ctx, 1, ctx->tx[1], ctx->rows[1], a, 0, false, d_err));
     }
     if (if_res) {
       for (int k = 0; k < G; ++k) {
@@ -1121,11 +1137,11 @@ int run(fwigb_ctx* ctx, int calc_id) {
       // then res_injection(nSteps-1) + el_stress_adj, source_grad(nSteps-2),
       // reverse velocity of step nSteps-2 ... (libCUFD.cu:353-445), with
       // backward iteration j meaning step nSteps_k - 2 - j of member k.
-      TIMED(3, launches += launch_sweep(ctx, 3, ctx->tx[3], G, -1, false, d_err));
+      TIMED(3, launches += launch_sweep(ctx, 3, ctx->tx[3], 1, G, -1, false, d_err));
       for (int j = 0; j <= ntop - 2; ++j) {
         const int a = active(j);
-        TIMED(2, launches += launch_sweep(ctx, 2, ctx->tx[2], a, j, false, d_err));
-        TIMED(3, launches += launch_sweep(ctx, 3, ctx->tx[3], a, j, false, d_err));
+        TIMED(2, launches += launch_sweep(ctx, 2, ctx->tx[2], 1, a, j, false, d_err));
+        TIMED(3, launches += launch_sweep(ctx, 3, ctx->tx[3], 1, a, j, false, d_err));
       }
     }
     if (adj || ctx->illum) {
@@ -1371,6 +1387,12 @@ long long fwigb_last_launch_count(const fwigb_ctx* ctx) { return ctx ? ctx->laun
 int fwigb_tile_config(const fwigb_ctx* ctx, int* tile_x) {
   if (!ctx || !tile_x) return FWIGB_ERR_ARG;
   for (int k = 0; k < 4; ++k) tile_x[k] = ctx->tx[k];
+  return FWIGB_OK;
+}
+
+int fwigb_tile_rows(const fwigb_ctx* ctx, int* rows) {
+  if (!ctx || !rows) return FWIGB_ERR_ARG;
+  for (int k = 0; k < 4; ++k) rows[k] = ctx->rows[k];
   return FWIGB_OK;
 }
 

@@ -15,15 +15,20 @@
 
 namespace fwigb {
 
-// Sweep tiles: 32 depths x TX columns, one cell per thread (block 32 x TX),
-// TX in {4, 8, 16} chosen per sweep by the autotuner.
+// Sweep tiles: backward sweeps 32 depths x TX columns, one cell per thread;
+// forward sweeps 64 depths x TX columns, two adjacent depths per thread
+// (block 32 x TX in both), TX in {4, 8, 16} chosen per sweep by the
+// autotuner.
 constexpr int kTileZ = 32;
+constexpr int kRowsFwd = 2;
+constexpr int kTileZFwd = kTileZ * kRowsFwd;
 // Receivers are binned on a fixed 32 x 8 grid, independent of the sweep tile.
 constexpr int kBinZ = 32;
 constexpr int kBinX = 8;
-// TMA box of one staged array: depths z0-4 .. z0+35 (start aligned to 16
-// bytes), columns x0-2 .. x0+TX+1.
+// TMA box of one staged array: depths z0-4 .. z0+tile+3 (start aligned to
+// 16 bytes), columns x0-2 .. x0+TX+1.
 constexpr int kBoxZ = kTileZ + 8;
+constexpr int kBoxZFwd = kTileZFwd + 8;
 constexpr int kTileXs[3] = {4, 8, 16};
 
 // Tensor maps of the (up to 5) arrays a sweep stages into shared memory.
@@ -54,19 +59,19 @@ struct Geo {
   float dt, rdz, rdx;
 };
 
-// Split of a sub-grid's tiles (32 depths x tx columns, ntz x ntx in all)
+// Split of a sub-grid's tiles (tz depths x tx columns, ntz x ntx in all)
 // into the fast tiles, the rectangle [ftz0, ftz1) x [ftx0, ftx1) of tiles
 // inside the fast box, and the edge tiles around it.
 struct TileSplit {
   int ntz, ntx, ftz0, ftz1, ftx0, ftx1;
 };
 
-__host__ __device__ inline TileSplit tile_split(const Geo& g, int tx) {
+__host__ __device__ inline TileSplit tile_split(const Geo& g, int tx, int tz) {
   TileSplit s;
-  s.ntz = (g.nz + kTileZ - 1) / kTileZ;
+  s.ntz = (g.nz + tz - 1) / tz;
   s.ntx = (g.nx + tx - 1) / tx;
-  s.ftz0 = (g.fz0 + kTileZ - 1) / kTileZ;
-  s.ftz1 = (g.fz1 + 1) / kTileZ;
+  s.ftz0 = (g.fz0 + tz - 1) / tz;
+  s.ftz1 = (g.fz1 + 1) / tz;
   s.ftx0 = (g.fx0 + tx - 1) / tx;
   s.ftx1 = (g.fx1 + 1) / tx;
   if (g.fz0 > g.fz1 || g.fx0 > g.fx1 || s.ftz1 <= s.ftz0 || s.ftx1 <= s.ftx0) s.ftz0 = s.ftz1 = s.ftx0 = s.ftx1 = 0;
@@ -143,7 +148,11 @@ struct ShotSlot {
 // sxx, sxz; B vz, vx, szz_a, sxx_a, sxz_a; C vz_a, vx_a, szz, sxx, sxz.
 struct SweepMaps {
   TileMaps f1, f2, b, c;
+  TileMaps f1w, f2w;  // forward sweeps with two-row tiles (kBoxZFwd boxes)
 };
+// Launch variants of the sweeps: 0 F1, 1 F2, 2 B, 3 C (one row per thread),
+// 4 F1, 5 F2 (two rows per thread).
+constexpr int kSweepVariants = 6;
 
 // What one sweep launch reads for up to K shots, passed by value as a
 // __grid_constant__ kernel parameter: the block of shot k reads its slot and
@@ -174,11 +183,13 @@ struct SweepGrid {
 // wait for its staged tiles gives up. The backward sweeps take the backward
 // iteration j; shot k works on its step nSteps_k - 2 - j. Instantiated for
 // K = 1 and K = kPackShots. Each returns the number of kernels it launched.
+// The forward launchers take the rows per thread (1 or 2; the pack's maps
+// must be the matching variant).
 template <int K>
-int launch_fwd_stress(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int it,
-                      bool save, unsigned* err);
+int launch_fwd_stress(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
+                      int it, bool save, unsigned* err);
 template <int K>
-int launch_fwd_velocity(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
+int launch_fwd_velocity(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
                         unsigned* err);
 template <int K>
 int launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,

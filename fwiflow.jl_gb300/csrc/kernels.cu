@@ -68,14 +68,14 @@ __device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* tm, i
 }
 
 // Starts staging NA arrays of the tile at (z0, x0) into shared memory: one
-// 2-D TMA copy each of the box [z0-4, z0+36) x [x0-2, x0+TX+2), zero filled
-// outside the grid. The leader initialises the mbarrier (fenced so the copies
-// see it) and issues the copies after the block has met the barrier's
+// 2-D TMA copy each of the box [z0-4, z0-4+BOXZ) x [x0-2, x0+TX+2), zero
+// filled outside the grid. The leader initialises the mbarrier (fenced so the
+// copies see it) and issues the copies after the block has met the barrier's
 // initialisation; the caller then loads its own-cell operands (which overlap
 // with the copies) and calls stage_wait.
-template <int NA, int TX>
+template <int NA, int TX, int BOXZ>
 __device__ __forceinline__ void stage_begin(const TileMaps& mp, float* sm, uint64_t* bar, int z0, int x0) {
-  constexpr int N = kBoxZ * (TX + 4);
+  constexpr int N = BOXZ * (TX + 4);
   const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
   if (leader) {
     mbar_init(bar, 1);
@@ -141,20 +141,20 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
 
 // Every sweep is one launch per time step for a pack of shots: blockIdx.z is
 // the shot (its slot holds its sub-grid, fields, source, receivers and TMA
-// maps), blockIdx.x / blockIdx.y the tile of 32 depths x TX columns. A tile
+// maps), blockIdx.x / blockIdx.y the tile of TZ depths x TX columns. A tile
 // inside the shot's fast rectangle runs the sweep's fast body (the interior
 // form of the reference kernels); any other tile runs its edge body (the
 // full CPML / boundary-ring / band logic). The choice is uniform per block.
 // Blocks past a narrower shot's grid leave before staging anything. Block
-// (32, TX), one cell per thread: lane threadIdx.x is the depth offset,
-// threadIdx.y the column offset; `b` is the cell's index in a staged box
-// (column stride kBoxZ).
-#define SWEEP_KERNEL_TILE()                                                    \
+// (32, TX): lane threadIdx.x covers R adjacent depths (R = TZ / 32),
+// threadIdx.y the column; `b` is the index of its first cell in a staged box
+// (column stride BOXZ = TZ + 8).
+#define SWEEP_KERNEL_TILE(TZ_)                                                 \
   const int shot = K == 1 ? 0 : static_cast<int>(blockIdx.z);                  \
   const Geo& g0 = P.slots[shot].g;                                             \
-  const int z0 = blockIdx.x * kTileZ, x0 = blockIdx.y * TX;                    \
+  const int z0 = blockIdx.x * (TZ_), x0 = blockIdx.y * TX;                     \
   if (z0 >= g0.nz || x0 >= g0.nx) return;                                      \
-  const TileSplit ts = tile_split(g0, TX);                                     \
+  const TileSplit ts = tile_split(g0, TX, (TZ_));                              \
   const bool fast = static_cast<int>(blockIdx.x) >= ts.ftz0 &&                 \
                     static_cast<int>(blockIdx.x) < ts.ftz1 &&                  \
                     static_cast<int>(blockIdx.y) >= ts.ftx0 &&                 \
@@ -166,149 +166,174 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
 
 // A fast tile lies wholly inside the grid. `special` marks the tiles that
 // meet the bounding box of the shot's receivers and source.
-#define SWEEP_FAST_SLOT()                                                      \
+#define SWEEP_FAST_SLOT(TZ_)                                                   \
   SWEEP_BODY_SLOT()                                                            \
   const ShotD& sh = S.sh;                                                      \
-  const bool special = !(z0 + kTileZ - 1 < sh.rbz0 || z0 > sh.rbz1 ||          \
+  const bool special = !(z0 + (TZ_) - 1 < sh.rbz0 || z0 > sh.rbz1 ||           \
                          x0 + TX - 1 < sh.rbx0 || x0 > sh.rbx1);
 
-#define SWEEP_STAGE(NA)                                                        \
-  constexpr int N = kBoxZ * (TX + 4);                                          \
+// Stages the tile and sets the thread's first cell (z, x), its global index
+// i and its box index b. A thread whose first cell is outside the grid
+// leaves (with R > 1 its later cells are checked by the edge body).
+#define SWEEP_STAGE(NA, BOXZ_, R_)                                             \
+  constexpr int N = (BOXZ_) * (TX + 4);                                        \
   extern __shared__ __align__(128) float sm[];                                 \
   __shared__ __align__(8) uint64_t bar;                                        \
-  stage_begin<NA, TX>(P.maps[shot], sm, &bar, z0, x0);                         \
+  stage_begin<NA, TX, (BOXZ_)>(P.maps[shot], sm, &bar, z0, x0);                \
   const Fields& f = S.f;                                                       \
   const MediaD& m = S.m;                                                       \
   const CpmlD& c = S.c;                                                        \
-  const int z = z0 + threadIdx.x, x = x0 + threadIdx.y;                        \
+  const int z = z0 + (R_) * static_cast<int>(threadIdx.x), x = x0 + threadIdx.y; \
   if (z >= g.nz || x >= g.nx) return;                                          \
   const size_t ldz = static_cast<size_t>(g.ldz);                               \
   const size_t i = static_cast<size_t>(x) * ldz + z;                           \
-  const int b = (threadIdx.y + 2) * kBoxZ + threadIdx.x + 4;                   \
+  const int b = (threadIdx.y + 2) * (BOXZ_) + (R_) * threadIdx.x + 4;          \
   (void)N;                                                                     \
   (void)b;                                                                     \
   (void)f;                                                                     \
   (void)m;                                                                     \
   (void)c;
 
+// Paired loads / stores of two adjacent depths (8-byte aligned: even depth,
+// ldz a multiple of 32, even box index).
+__device__ __forceinline__ float2 ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void st2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
+
+// 4th-order staggered difference from its four samples: (C1 (p - q) -
+// C2 (s - t)) r, the expression of sdm / sdp.
+__device__ __forceinline__ float dd(float p, float q, float s, float t, float r) {
+  return (C1 * (p - q) - C2 * (s - t)) * r;
+}
+
 // Register budgets (measured on GB300 over the tile widths): forward sweeps
-// 32 registers (64 warps per SM), backward sweeps 48 (40 warps per SM; more
-// resident warps beat the loads the compiler could otherwise hoist).
-#define FWD_BOUNDS __launch_bounds__(32 * TX, 2048 / (32 * TX))
+// 32 registers with one cell per thread (64 warps per SM) and 40 with two,
+// backward sweeps 48 (40 warps per SM; more resident warps beat the loads the
+// compiler could otherwise hoist).
+#define FWD_BOUNDS __launch_bounds__(32 * TX, (R == 1 ? 2048 : 1536) / (32 * TX))
 #define BWD_BOUNDS __launch_bounds__(32 * TX, (1280 / (32 * TX)) > 0 ? (1280 / (32 * TX)) : 1)
 
 // ---------------------------------------------------------------------------
 // F1: el_stress (el_stress.cu:50-88) + add_source (utilities.cu:521-541) +
 // recording (utilities.cu:557-567) + from_bnd of the 5 fields (Boundary.cu:55-76).
-// Staged: vz, vx.
-template <int TX, int K>
-__device__ __forceinline__ void fwd_stress_edge(const SweepPack<K>& P, int shot, int z0, int x0, int it, int save, unsigned* err) {
+// Staged: vz, vx. Edge body: the per-cell code for each of the thread's R
+// depths (after the staged tiles have landed).
+template <int TX, int K, int R>
+__device__ __forceinline__ void fwd_stress_edge(const SweepPack<K>& P, int shot, int z0, int x0, int it, int save,
+                                                unsigned* err) {
+  constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
-  SWEEP_STAGE(2)
+  SWEEP_STAGE(2, BOXZ, R)
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
-  float szz = f.szz[i], sxx = f.sxx[i], sxz = f.sxz[i];
-  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
   if (!stage_wait(&bar, err)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
-  if (save) {
-    const int k = ring_index(g, z, x);
-    if (k >= 0) {
-      float* p = st.base + static_cast<size_t>(it) * 5 * g.ring_len + k;
-      p[0] = szz;
-      p[g.ring_len] = sxz;
-      p[2 * g.ring_len] = sxx;
-      p[3 * g.ring_len] = s_vz[b];
-      p[4 * g.ring_len] = s_vx[b];
+  auto cell = [&](const int z, const size_t i, const int b) {
+    float szz = f.szz[i], sxx = f.sxx[i];
+    const float sxz = f.sxz[i];
+    const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
+    if (save) {
+      const int k = ring_index(g, z, x);
+      if (k >= 0) {
+        float* p = st.base + static_cast<size_t>(it) * 5 * g.ring_len + k;
+        p[0] = szz;
+        p[g.ring_len] = sxz;
+        p[2 * g.ring_len] = sxx;
+        p[3 * g.ring_len] = s_vz[b];
+        p[4 * g.ring_len] = s_vx[b];
+      }
     }
-  }
-  const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
-  const bool src = (z == sh.src_z && x == sh.src_x);
-  if (dom) {
-    float dvz_dz = sdm(s_vz, b, 1, g.rdz);
-    float dvx_dx = sdm(s_vx, b, kBoxZ, g.rdx);
-    float dvx_dz = sdp(s_vx, b, 1, g.rdz);
-    float dvz_dx = sdp(s_vz, b, kBoxZ, g.rdx);
-    if ((z < g.nPml) || (z > g.zpml_hi)) {
-      float mm = c.b_z[z] * f.m_dvz_dz[i] + c.a_z[z] * dvz_dz;
-      f.m_dvz_dz[i] = mm;
-      dvz_dz = dvz_dz / c.K_z[z] + mm;
-      mm = c.b_zh[z] * f.m_dvx_dz[i] + c.a_zh[z] * dvx_dz;
-      f.m_dvx_dz[i] = mm;
-      dvx_dz = dvx_dz / c.K_zh[z] + mm;
+    const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
+    const bool src = (z == sh.src_z && x == sh.src_x);
+    if (dom) {
+      float dvz_dz = sdm(s_vz, b, 1, g.rdz);
+      float dvx_dx = sdm(s_vx, b, BOXZ, g.rdx);
+      float dvx_dz = sdp(s_vx, b, 1, g.rdz);
+      float dvz_dx = sdp(s_vz, b, BOXZ, g.rdx);
+      if ((z < g.nPml) || (z > g.zpml_hi)) {
+        float mm = c.b_z[z] * f.m_dvz_dz[i] + c.a_z[z] * dvz_dz;
+        f.m_dvz_dz[i] = mm;
+        dvz_dz = dvz_dz / c.K_z[z] + mm;
+        mm = c.b_zh[z] * f.m_dvx_dz[i] + c.a_zh[z] * dvx_dz;
+        f.m_dvx_dz[i] = mm;
+        dvx_dz = dvx_dz / c.K_zh[z] + mm;
+      }
+      if ((x < g.nPml) || (x > g.xpml_hi_s)) {
+        float mm = c.b_x[x] * f.m_dvx_dx[i] + c.a_x[x] * dvx_dx;
+        f.m_dvx_dx[i] = mm;
+        dvx_dx = dvx_dx / c.K_x[x] + mm;
+        mm = c.b_xh[x] * f.m_dvz_dx[i] + c.a_xh[x] * dvz_dx;
+        f.m_dvz_dx[i] = mm;
+        dvz_dx = dvz_dx / c.K_xh[x] + mm;
+      }
+      szz += (l2m * dvz_dz + lam * dvx_dx) * g.dt;
+      sxx += (lam * dvz_dz + l2m * dvx_dx) * g.dt;
+      f.sxz[i] = sxz + amu * (dvx_dz + dvz_dx) * g.dt;
     }
-    if ((x < g.nPml) || (x > g.xpml_hi_s)) {
-      float mm = c.b_x[x] * f.m_dvx_dx[i] + c.a_x[x] * dvx_dx;
-      f.m_dvx_dx[i] = mm;
-      dvx_dx = dvx_dx / c.K_x[x] + mm;
-      mm = c.b_xh[x] * f.m_dvz_dx[i] + c.a_xh[x] * dvz_dx;
-      f.m_dvz_dx[i] = mm;
-      dvz_dx = dvz_dx / c.K_xh[x] + mm;
+    if (src) {
+      szz += sh.src_szz[it];
+      sxx += sh.src_sxx[it];
     }
-    szz += (l2m * dvz_dz + lam * dvx_dx) * g.dt;
-    sxx += (lam * dvz_dz + l2m * dvx_dx) * g.dt;
-    f.sxz[i] = sxz + amu * (dvx_dz + dvz_dx) * g.dt;
-  }
-  if (src) {
-    szz += sh.src_szz[it];
-    sxx += sh.src_sxx[it];
-  }
-  if (dom || src) {
-    f.szz[i] = szz;
-    f.sxx[i] = sxx;
-  }
-  // The velocity sweep that follows does not change the stresses, so the
-  // sample of step it+1 is taken here.
-  const int2 rr = bin_range(sh, z, x);
-  for (int k = rr.x; k < rr.y; ++k) {
-    const int r = sh.blk_rec[k];
-    if (sh.rec_z[r] == z && sh.rec_x[r] == x) sh.data[static_cast<size_t>(r) * sh.nSteps + it + 1] = szz + 3.0f * sxx;
-  }
+    if (dom || src) {
+      f.szz[i] = szz;
+      f.sxx[i] = sxx;
+    }
+    // The velocity sweep that follows does not change the stresses, so the
+    // sample of step it+1 is taken here.
+    const int2 rr = bin_range(sh, z, x);
+    for (int k = rr.x; k < rr.y; ++k) {
+      const int r = sh.blk_rec[k];
+      if (sh.rec_z[r] == z && sh.rec_x[r] == x)
+        sh.data[static_cast<size_t>(r) * sh.nSteps + it + 1] = szz + 3.0f * sxx;
+    }
+  };
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (z + r < g.nz) cell(z + r, i + r, b + r);
 }
 
 // F2: el_velocity, isFor = true (el_velocity.cu:45-82). Staged: szz, sxx, sxz.
-template <int TX, int K>
+template <int TX, int K, int R>
 __device__ __forceinline__ void fwd_velocity_edge(const SweepPack<K>& P, int shot, int z0, int x0, unsigned* err) {
+  constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
-  SWEEP_STAGE(3)
-  const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
-  float vz = 0.0f, vx = 0.0f, bA = 0.0f, bB = 0.0f;
-  if (dom) {
-    vz = f.vz[i];
-    vx = f.vx[i];
-    bA = m.bycA[i];
-    bB = m.bycB[i];
-  }
-  if (!stage_wait(&bar, err) || !dom) return;
+  SWEEP_STAGE(3, BOXZ, R)
+  if (!stage_wait(&bar, err)) return;
   const float* s_szz = sm;
   const float* s_sxx = sm + N;
   const float* s_sxz = sm + 2 * N;
-  float dszz_dz = sdp(s_szz, b, 1, g.rdz);
-  float dsxz_dx = sdm(s_sxz, b, kBoxZ, g.rdx);
-  float dsxz_dz = sdm(s_sxz, b, 1, g.rdz);
-  float dsxx_dx = sdp(s_sxx, b, kBoxZ, g.rdx);
-  if ((z < g.nPml) || (z > g.zpml_hi)) {
-    float mm = c.b_zh[z] * f.m_dszz_dz[i] + c.a_zh[z] * dszz_dz;
-    f.m_dszz_dz[i] = mm;
-    dszz_dz = dszz_dz / c.K_zh[z] + mm;
-    mm = c.b_z[z] * f.m_dsxz_dz[i] + c.a_z[z] * dsxz_dz;
-    f.m_dsxz_dz[i] = mm;
-    dsxz_dz = dsxz_dz / c.K_z[z] + mm;
-  }
-  if ((x < g.nPml) || (x > g.xpml_hi_v)) {
-    float mm = c.b_x[x] * f.m_dsxz_dx[i] + c.a_x[x] * dsxz_dx;
-    f.m_dsxz_dx[i] = mm;
-    dsxz_dx = dsxz_dx / c.K_x[x] + mm;
-    mm = c.b_xh[x] * f.m_dsxx_dx[i] + c.a_xh[x] * dsxx_dx;
-    f.m_dsxx_dx[i] = mm;
-    dsxx_dx = dsxx_dx / c.K_xh[x] + mm;
-  }
-  const float nvz = vz + (dszz_dz + dsxz_dx) * bA * g.dt;
-  const float nvx = vx + (dsxz_dz + dsxx_dx) * bB * g.dt;
-  f.vz[i] = nvz;
-  f.vx[i] = nvx;
-  if (S.gr.illum) S.gr.illum[i] += nvz * nvz + nvx * nvx;
+  auto cell = [&](const int z, const size_t i, const int b) {
+    if (!in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1)) return;
+    const float vz = f.vz[i], vx = f.vx[i], bA = m.bycA[i], bB = m.bycB[i];
+    float dszz_dz = sdp(s_szz, b, 1, g.rdz);
+    float dsxz_dx = sdm(s_sxz, b, BOXZ, g.rdx);
+    float dsxz_dz = sdm(s_sxz, b, 1, g.rdz);
+    float dsxx_dx = sdp(s_sxx, b, BOXZ, g.rdx);
+    if ((z < g.nPml) || (z > g.zpml_hi)) {
+      float mm = c.b_zh[z] * f.m_dszz_dz[i] + c.a_zh[z] * dszz_dz;
+      f.m_dszz_dz[i] = mm;
+      dszz_dz = dszz_dz / c.K_zh[z] + mm;
+      mm = c.b_z[z] * f.m_dsxz_dz[i] + c.a_z[z] * dsxz_dz;
+      f.m_dsxz_dz[i] = mm;
+      dsxz_dz = dsxz_dz / c.K_z[z] + mm;
+    }
+    if ((x < g.nPml) || (x > g.xpml_hi_v)) {
+      float mm = c.b_x[x] * f.m_dsxz_dx[i] + c.a_x[x] * dsxz_dx;
+      f.m_dsxz_dx[i] = mm;
+      dsxz_dx = dsxz_dx / c.K_x[x] + mm;
+      mm = c.b_xh[x] * f.m_dsxx_dx[i] + c.a_xh[x] * dsxx_dx;
+      f.m_dsxx_dx[i] = mm;
+      dsxx_dx = dsxx_dx / c.K_xh[x] + mm;
+    }
+    const float nvz = vz + (dszz_dz + dsxz_dx) * bA * g.dt;
+    const float nvx = vx + (dsxz_dz + dsxx_dx) * bB * g.dt;
+    f.vz[i] = nvz;
+    f.vx[i] = nvx;
+    if (S.gr.illum) S.gr.illum[i] += nvz * nvz + nvx * nvx;
+  };
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (z + r < g.nz) cell(z + r, i + r, b + r);
 }
 
 // ---------------------------------------------------------------------------
@@ -317,7 +342,7 @@ __device__ __forceinline__ void fwd_velocity_edge(const SweepPack<K>& P, int sho
 template <int TX, int K>
 __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   SWEEP_BODY_SLOT()
-  SWEEP_STAGE(5)
+  SWEEP_STAGE(5, kBoxZ, 1)
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
   const Grads& gr = S.gr;
@@ -435,7 +460,7 @@ __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int 
 template <int TX, int K>
 __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   SWEEP_BODY_SLOT()
-  SWEEP_STAGE(5)
+  SWEEP_STAGE(5, kBoxZ, 1)
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
   const Grads& gr = S.gr;
@@ -560,10 +585,11 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
 // box of the shot's receivers and source. Operation order otherwise follows
 // the edge kernels.
 
+// Forward fast bodies, one depth per thread (32-row tiles).
 template <int TX, int K>
-__device__ __forceinline__ void fwd_stress_fast(const SweepPack<K>& P, int shot, int z0, int x0, int it, unsigned* err) {
-  SWEEP_FAST_SLOT()
-  SWEEP_STAGE(2)
+__device__ __forceinline__ void fwd_stress_fast1(const SweepPack<K>& P, int shot, int z0, int x0, int it, unsigned* err) {
+  SWEEP_FAST_SLOT(kTileZ)
+  SWEEP_STAGE(2, kBoxZ, 1)
   float szz = f.szz[i], sxx = f.sxx[i];
   const float sxz = f.sxz[i];
   const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
@@ -594,10 +620,10 @@ __device__ __forceinline__ void fwd_stress_fast(const SweepPack<K>& P, int shot,
 }
 
 template <int TX, int K>
-__device__ __forceinline__ void fwd_velocity_fast(const SweepPack<K>& P, int shot, int z0, int x0, unsigned* err) {
-  SWEEP_FAST_SLOT()
+__device__ __forceinline__ void fwd_velocity_fast1(const SweepPack<K>& P, int shot, int z0, int x0, unsigned* err) {
+  SWEEP_FAST_SLOT(kTileZ)
   (void)special;
-  SWEEP_STAGE(3)
+  SWEEP_STAGE(3, kBoxZ, 1)
   const float vz = f.vz[i], vx = f.vx[i], bA = m.bycA[i], bB = m.bycB[i];
   if (!stage_wait(&bar, err)) return;
   const float* s_szz = sm;
@@ -614,10 +640,98 @@ __device__ __forceinline__ void fwd_velocity_fast(const SweepPack<K>& P, int sho
   if (S.gr.illum) S.gr.illum[i] += nvz * nvz + nvx * nvx;
 }
 
+// Forward fast bodies, two adjacent depths per thread (R = 2): own-cell
+// operands and results move as float2, and the staged samples are read in
+// pairs (b-2, b-1), (b, b+1), (b+2, b+3) along z and (b, b+1) at each
+// column offset along x, which cover the stencils of both depths.
+template <int TX, int K, int R>
+__device__ __forceinline__ void fwd_stress_fast2(const SweepPack<K>& P, int shot, int z0, int x0, int it,
+                                                 unsigned* err) {
+  static_assert(R == 2, "the forward fast bodies handle two depths per thread");
+  constexpr int TZ = 32 * R, BOXZ = TZ + 8;
+  SWEEP_FAST_SLOT(TZ)
+  SWEEP_STAGE(2, BOXZ, R)
+  const float2 szz = ld2(f.szz + i), sxx = ld2(f.sxx + i), sxz = ld2(f.sxz + i);
+  const float2 lam = ld2(m.lam + i), l2m = ld2(m.l2m + i), amu = ld2(m.aveMu + i);
+  if (!stage_wait(&bar, err)) return;
+  const float* s_vz = sm;
+  const float* s_vx = sm + N;
+  const float rdz = g.rdz, rdx = g.rdx, dt = g.dt;
+  const float2 zm = ld2(s_vz + b - 2), z0v = ld2(s_vz + b), zp = ld2(s_vz + b + 2);
+  const float2 xm = ld2(s_vx + b - 2), x0v = ld2(s_vx + b), xp = ld2(s_vx + b + 2);
+  const float2 zc1 = ld2(s_vz + b + BOXZ), zc2 = ld2(s_vz + b + 2 * BOXZ), zcm = ld2(s_vz + b - BOXZ);
+  const float2 xc1 = ld2(s_vx + b + BOXZ), xcm = ld2(s_vx + b - BOXZ), xcm2 = ld2(s_vx + b - 2 * BOXZ);
+  // depth z (.x): sdm_z(vz) = dd(a[b], a[b-1], a[b+1], a[b-2]); sdp_z(vx) = dd(a[b+1], a[b], a[b+2], a[b-1])
+  const float dvz_dz0 = dd(z0v.x, zm.y, z0v.y, zm.x, rdz), dvz_dz1 = dd(z0v.y, z0v.x, zp.x, zm.y, rdz);
+  const float dvx_dz0 = dd(x0v.y, x0v.x, xp.x, xm.y, rdz), dvx_dz1 = dd(xp.x, x0v.y, xp.y, x0v.x, rdz);
+  // along x: sdm_x(vx) = dd(a[b], a[b-B], a[b+B], a[b-2B]); sdp_x(vz) = dd(a[b+B], a[b], a[b+2B], a[b-B])
+  const float dvx_dx0 = dd(x0v.x, xcm.x, xc1.x, xcm2.x, rdx), dvx_dx1 = dd(x0v.y, xcm.y, xc1.y, xcm2.y, rdx);
+  const float dvz_dx0 = dd(zc1.x, z0v.x, zc2.x, zcm.x, rdx), dvz_dx1 = dd(zc1.y, z0v.y, zc2.y, zcm.y, rdx);
+  float szz0 = szz.x + (l2m.x * dvz_dz0 + lam.x * dvx_dx0) * dt;
+  float szz1 = szz.y + (l2m.y * dvz_dz1 + lam.y * dvx_dx1) * dt;
+  float sxx0 = sxx.x + (lam.x * dvz_dz0 + l2m.x * dvx_dx0) * dt;
+  float sxx1 = sxx.y + (lam.y * dvz_dz1 + l2m.y * dvx_dx1) * dt;
+  st2(f.sxz + i, sxz.x + amu.x * (dvx_dz0 + dvz_dx0) * dt, sxz.y + amu.y * (dvx_dz1 + dvz_dx1) * dt);
+  if (special) {
+    float* szr[2] = {&szz0, &szz1};
+    float* sxr[2] = {&sxx0, &sxx1};
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int zr = z + r;
+      if (zr == sh.src_z && x == sh.src_x) {
+        *szr[r] += sh.src_szz[it];
+        *sxr[r] += sh.src_sxx[it];
+      }
+      const int2 rr = bin_range(sh, zr, x);
+      for (int k = rr.x; k < rr.y; ++k) {
+        const int q = sh.blk_rec[k];
+        if (sh.rec_z[q] == zr && sh.rec_x[q] == x)
+          sh.data[static_cast<size_t>(q) * sh.nSteps + it + 1] = *szr[r] + 3.0f * *sxr[r];
+      }
+    }
+  }
+  st2(f.szz + i, szz0, szz1);
+  st2(f.sxx + i, sxx0, sxx1);
+}
+
+template <int TX, int K, int R>
+__device__ __forceinline__ void fwd_velocity_fast2(const SweepPack<K>& P, int shot, int z0, int x0, unsigned* err) {
+  static_assert(R == 2, "the forward fast bodies handle two depths per thread");
+  constexpr int TZ = 32 * R, BOXZ = TZ + 8;
+  SWEEP_FAST_SLOT(TZ)
+  (void)special;
+  SWEEP_STAGE(3, BOXZ, R)
+  const float2 vz = ld2(f.vz + i), vx = ld2(f.vx + i), bA = ld2(m.bycA + i), bB = ld2(m.bycB + i);
+  if (!stage_wait(&bar, err)) return;
+  const float* s_szz = sm;
+  const float* s_sxx = sm + N;
+  const float* s_sxz = sm + 2 * N;
+  const float rdz = g.rdz, rdx = g.rdx, dt = g.dt;
+  const float2 pm = ld2(s_szz + b - 2), p0 = ld2(s_szz + b), pp = ld2(s_szz + b + 2);
+  const float2 qm = ld2(s_sxz + b - 2), q0 = ld2(s_sxz + b), qp = ld2(s_sxz + b + 2);
+  const float2 qcm = ld2(s_sxz + b - BOXZ), qc1 = ld2(s_sxz + b + BOXZ), qcm2 = ld2(s_sxz + b - 2 * BOXZ);
+  const float2 r0 = ld2(s_sxx + b), rc1 = ld2(s_sxx + b + BOXZ), rc2 = ld2(s_sxx + b + 2 * BOXZ),
+               rcm = ld2(s_sxx + b - BOXZ);
+  // sdp_z(szz) = dd(a[b+1], a[b], a[b+2], a[b-1]); sdm_x(sxz) = dd(a[b], a[b-B], a[b+B], a[b-2B]);
+  // sdm_z(sxz) = dd(a[b], a[b-1], a[b+1], a[b-2]); sdp_x(sxx) = dd(a[b+B], a[b], a[b+2B], a[b-B])
+  const float dszz_dz0 = dd(p0.y, p0.x, pp.x, pm.y, rdz), dszz_dz1 = dd(pp.x, p0.y, pp.y, p0.x, rdz);
+  const float dsxz_dx0 = dd(q0.x, qcm.x, qc1.x, qcm2.x, rdx), dsxz_dx1 = dd(q0.y, qcm.y, qc1.y, qcm2.y, rdx);
+  const float dsxz_dz0 = dd(q0.x, qm.y, q0.y, qm.x, rdz), dsxz_dz1 = dd(q0.y, q0.x, qp.x, qm.y, rdz);
+  const float dsxx_dx0 = dd(rc1.x, r0.x, rc2.x, rcm.x, rdx), dsxx_dx1 = dd(rc1.y, r0.y, rc2.y, rcm.y, rdx);
+  const float nvz0 = vz.x + (dszz_dz0 + dsxz_dx0) * bA.x * dt, nvz1 = vz.y + (dszz_dz1 + dsxz_dx1) * bA.y * dt;
+  const float nvx0 = vx.x + (dsxz_dz0 + dsxx_dx0) * bB.x * dt, nvx1 = vx.y + (dsxz_dz1 + dsxx_dx1) * bB.y * dt;
+  st2(f.vz + i, nvz0, nvz1);
+  st2(f.vx + i, nvx0, nvx1);
+  if (S.gr.illum) {
+    const float2 e = ld2(S.gr.illum + i);
+    st2(S.gr.illum + i, e.x + (nvz0 * nvz0 + nvx0 * nvx0), e.y + (nvz1 * nvz1 + nvx1 * nvx1));
+  }
+}
+
 template <int TX, int K>
 __device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
-  SWEEP_FAST_SLOT()
-  SWEEP_STAGE(5)
+  SWEEP_FAST_SLOT(kTileZ)
+  SWEEP_STAGE(5, kBoxZ, 1)
   const Grads& gr = S.gr;
   const int it = S.nSteps - 2 - j;
   const float dt = g.dt;
@@ -683,8 +797,8 @@ __device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int 
 
 template <int TX, int K>
 __device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
-  SWEEP_FAST_SLOT()
-  SWEEP_STAGE(5)
+  SWEEP_FAST_SLOT(kTileZ)
+  SWEEP_STAGE(5, kBoxZ, 1)
   const Grads& gr = S.gr;
   const int it = S.nSteps - 2 - j;
   const int rev = it >= 1;
@@ -756,27 +870,37 @@ __device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int 
 // ---------------------------------------------------------------------------
 // The sweep kernels: one launch per sweep and time step.
 
-template <int TX, int K>
+// Forward sweeps: R depths per thread (tiles of 32 R rows), R in {1, 2}
+// picked per workload by the autotuner.
+template <int TX, int K, int R>
 __global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ SweepPack<K> P, int it, int save, unsigned* err) {
-  SWEEP_KERNEL_TILE()
-  if (fast)
-    fwd_stress_fast<TX, K>(P, shot, z0, x0, it, err);
-  else
-    fwd_stress_edge<TX, K>(P, shot, z0, x0, it, save, err);
+  SWEEP_KERNEL_TILE(32 * R)
+  if (fast) {
+    if constexpr (R == 1)
+      fwd_stress_fast1<TX, K>(P, shot, z0, x0, it, err);
+    else
+      fwd_stress_fast2<TX, K, R>(P, shot, z0, x0, it, err);
+  } else {
+    fwd_stress_edge<TX, K, R>(P, shot, z0, x0, it, save, err);
+  }
 }
 
-template <int TX, int K>
+template <int TX, int K, int R>
 __global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ SweepPack<K> P, unsigned* err) {
-  SWEEP_KERNEL_TILE()
-  if (fast)
-    fwd_velocity_fast<TX, K>(P, shot, z0, x0, err);
-  else
-    fwd_velocity_edge<TX, K>(P, shot, z0, x0, err);
+  SWEEP_KERNEL_TILE(32 * R)
+  if (fast) {
+    if constexpr (R == 1)
+      fwd_velocity_fast1<TX, K>(P, shot, z0, x0, err);
+    else
+      fwd_velocity_fast2<TX, K, R>(P, shot, z0, x0, err);
+  } else {
+    fwd_velocity_edge<TX, K, R>(P, shot, z0, x0, err);
+  }
 }
 
 template <int TX, int K>
 __global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
-  SWEEP_KERNEL_TILE()
+  SWEEP_KERNEL_TILE(kTileZ)
   if (fast)
     bwd_B_fast<TX, K>(P, shot, z0, x0, j, err);
   else
@@ -785,7 +909,7 @@ __global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ SweepPack<K> P, int j
 
 template <int TX, int K>
 __global__ void BWD_BOUNDS k_bwd_C(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
-  SWEEP_KERNEL_TILE()
+  SWEEP_KERNEL_TILE(kTileZ)
   if (fast)
     bwd_C_fast<TX, K>(P, shot, z0, x0, j, err);
   else
@@ -959,9 +1083,9 @@ __global__ void k_sum_partials(const double* __restrict__ partials, int n, doubl
 // ---------------------------------------------------------------------------
 namespace {
 
-template <int TX>
+template <int TX, int BOXZ>
 constexpr size_t smem_bytes(int na) {
-  return static_cast<size_t>(na) * kBoxZ * (TX + 4) * sizeof(float);
+  return static_cast<size_t>(na) * BOXZ * (TX + 4) * sizeof(float);
 }
 
 }  // namespace
@@ -985,30 +1109,38 @@ constexpr size_t smem_bytes(int na) {
     }                              \
   }
 
-dim3 sweep_grid(int tx, const SweepGrid& gr, int nshots) {
-  return dim3((gr.nz + kTileZ - 1) / kTileZ, (gr.nx + tx - 1) / tx, nshots);
+dim3 sweep_grid(int tx, int tz, const SweepGrid& gr, int nshots) {
+  return dim3((gr.nz + tz - 1) / tz, (gr.nx + tx - 1) / tx, nshots);
 }
 
 template <int K>
-int launch_fwd_stress(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int it,
+int launch_fwd_stress(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int it,
                       bool save, unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, k_fwd_stress<TX, K><<<sweep_grid(TX, gr, nshots), dim3(32, TX), smem_bytes<TX>(2), s>>>(
-                            p, it, save ? 1 : 0, err))
+  if (rows == 2)
+    FWIGB_DISPATCH_TX(tx, k_fwd_stress<TX, K, 2><<<sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
+                                                   smem_bytes<TX, kBoxZFwd>(2), s>>>(p, it, save ? 1 : 0, err))
+  else
+    FWIGB_DISPATCH_TX(tx, k_fwd_stress<TX, K, 1><<<sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+                                                   smem_bytes<TX, kBoxZ>(2), s>>>(p, it, save ? 1 : 0, err))
   return 1;
 }
 
 template <int K>
-int launch_fwd_velocity(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
+int launch_fwd_velocity(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
                         unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, k_fwd_velocity<TX, K><<<sweep_grid(TX, gr, nshots), dim3(32, TX), smem_bytes<TX>(3), s>>>(
-                            p, err))
+  if (rows == 2)
+    FWIGB_DISPATCH_TX(tx, k_fwd_velocity<TX, K, 2><<<sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
+                                                     smem_bytes<TX, kBoxZFwd>(3), s>>>(p, err))
+  else
+    FWIGB_DISPATCH_TX(tx, k_fwd_velocity<TX, K, 1><<<sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+                                                     smem_bytes<TX, kBoxZ>(3), s>>>(p, err))
   return 1;
 }
 
 template <int K>
 int launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, k_bwd_B<TX, K><<<sweep_grid(TX, gr, nshots), dim3(32, TX), smem_bytes<TX>(5), s>>>(p, j,
+  FWIGB_DISPATCH_TX(tx, k_bwd_B<TX, K><<<sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX), smem_bytes<TX, kBoxZ>(5), s>>>(p, j,
                                                                                                          err))
   return 1;
 }
@@ -1016,15 +1148,16 @@ int launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, cons
 template <int K>
 int launch_bwd_C(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, k_bwd_C<TX, K><<<sweep_grid(TX, gr, nshots), dim3(32, TX), smem_bytes<TX>(5), s>>>(p, j,
+  FWIGB_DISPATCH_TX(tx, k_bwd_C<TX, K><<<sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX), smem_bytes<TX, kBoxZ>(5), s>>>(p, j,
                                                                                                          err))
   return 1;
 }
 
 #define FWIGB_INSTANTIATE(K)                                                                                    \
-  template int launch_fwd_stress<K>(cudaStream_t, int, const SweepPack<K>&, int, const SweepGrid&, int, bool,    \
+  template int launch_fwd_stress<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&, int, bool, \
                                     unsigned*);                                                                  \
-  template int launch_fwd_velocity<K>(cudaStream_t, int, const SweepPack<K>&, int, const SweepGrid&, unsigned*); \
+  template int launch_fwd_velocity<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&,        \
+                                      unsigned*);                                                                \
   template int launch_bwd_B<K>(cudaStream_t, int, const SweepPack<K>&, int, const SweepGrid&, int, unsigned*);   \
   template int launch_bwd_C<K>(cudaStream_t, int, const SweepPack<K>&, int, const SweepGrid&, int, unsigned*);
 FWIGB_INSTANTIATE(1)
@@ -1032,10 +1165,11 @@ FWIGB_INSTANTIATE(kPackShots)
 #undef FWIGB_INSTANTIATE
 
 // Tensor maps: one per staged array, a 2-D view (z inner, x outer; row stride
-// ldz floats) with the box kBoxZ x (TX + 4). cuTensorMapEncodeTiled checks
-// the base (16-byte aligned: every array starts a multiple of ldz*nx floats
-// into a 256-byte aligned allocation) and the stride (ldz*4, a multiple of
-// 128); the x coordinate of every copy, z0 - 4 with z0 a multiple of 32, is a
+// ldz floats) with the box kBoxZ x (TX + 4), and kBoxZFwd x (TX + 4) for
+// the two-row forward sweeps. cuTensorMapEncodeTiled checks the
+// base (16-byte aligned: every array starts a multiple of ldz*nx floats into
+// a 256-byte aligned allocation) and the stride (ldz*4, a multiple of 128);
+// the x coordinate of every copy, z0 - 4 with z0 a multiple of 32, is a
 // multiple of 4 floats.
 bool encode_sweep_maps(const Geo& g, const Fields& f, int tx, SweepMaps& out, const char** err) {
   // g is the shot's sub-grid; f its fields.
@@ -1055,23 +1189,26 @@ bool encode_sweep_maps(const Geo& g, const Fields& f, int tx, SweepMaps& out, co
     *err = "column stride is not a multiple of 32 floats";
     return false;
   }
-  auto one = [&](CUtensorMap* m, float* base) {
+  auto one = [&](CUtensorMap* m, float* base, int boxz) {
     if (reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
     const cuuint64_t dims[2] = {static_cast<cuuint64_t>(g.nz), static_cast<cuuint64_t>(g.nx)};
     const cuuint64_t strides[1] = {static_cast<cuuint64_t>(g.ldz) * sizeof(float)};
-    const cuuint32_t box[2] = {static_cast<cuuint32_t>(kBoxZ), static_cast<cuuint32_t>(tx + 4)};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(boxz), static_cast<cuuint32_t>(tx + 4)};
     const cuuint32_t estr[2] = {1, 1};
     return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
   };
   bool ok = true;
-  ok = ok && one(&out.f1.t[0], f.vz) && one(&out.f1.t[1], f.vx);
-  ok = ok && one(&out.f2.t[0], f.szz) && one(&out.f2.t[1], f.sxx) && one(&out.f2.t[2], f.sxz);
-  ok = ok && one(&out.b.t[0], f.vz) && one(&out.b.t[1], f.vx) && one(&out.b.t[2], f.szz_a) &&
-       one(&out.b.t[3], f.sxx_a) && one(&out.b.t[4], f.sxz_a);
-  ok = ok && one(&out.c.t[0], f.vz_a) && one(&out.c.t[1], f.vx_a) && one(&out.c.t[2], f.szz) &&
-       one(&out.c.t[3], f.sxx) && one(&out.c.t[4], f.sxz);
+  const int F = kBoxZFwd, B = kBoxZ;
+  ok = ok && one(&out.f1.t[0], f.vz, B) && one(&out.f1.t[1], f.vx, B);
+  ok = ok && one(&out.f2.t[0], f.szz, B) && one(&out.f2.t[1], f.sxx, B) && one(&out.f2.t[2], f.sxz, B);
+  ok = ok && one(&out.f1w.t[0], f.vz, F) && one(&out.f1w.t[1], f.vx, F);
+  ok = ok && one(&out.f2w.t[0], f.szz, F) && one(&out.f2w.t[1], f.sxx, F) && one(&out.f2w.t[2], f.sxz, F);
+  ok = ok && one(&out.b.t[0], f.vz, B) && one(&out.b.t[1], f.vx, B) && one(&out.b.t[2], f.szz_a, B) &&
+       one(&out.b.t[3], f.sxx_a, B) && one(&out.b.t[4], f.sxz_a, B);
+  ok = ok && one(&out.c.t[0], f.vz_a, B) && one(&out.c.t[1], f.vx_a, B) && one(&out.c.t[2], f.szz, B) &&
+       one(&out.c.t[3], f.sxx, B) && one(&out.c.t[4], f.sxz, B);
   if (!ok) *err = "cuTensorMapEncodeTiled rejected a sweep tile";
   return ok;
 }

@@ -206,6 +206,12 @@ class FwiContext:
         _lib.check(self._lib.fwigb_tile_config(self._h, _lib.iptr(t)), self._h)
         return [int(v) for v in t]
 
+    def tile_rows(self):
+        """Depths per thread of (forward stress, forward velocity, backward B, backward C)."""
+        t = np.zeros(4, dtype=np.int32)
+        _lib.check(self._lib.fwigb_tile_rows(self._h, _lib.iptr(t)), self._h)
+        return [int(v) for v in t]
+
     def set_tile_config(self, widths=None) -> None:
         """Fix the four tile widths (4, 8 or 16); None re-enables the autotuner."""
         t = None if widths is None else np.ascontiguousarray(widths, dtype=np.int32)
