@@ -66,6 +66,10 @@ SIGNATURES = {
     "fwigb_cnn_conv3x3": ([_V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _V, _V, _V, _V,
                            _V, _V, _V], ctypes.c_int),
     "fwigb_cnn_tile_count": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "fwigb_cnn_conv3x3_tc": ([_V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _V, _V, _V, _V, _V, _V,
+                              _V], ctypes.c_int),
+    "fwigb_cnn_pack_weights_tc": ([_V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _V,
+                                   _V], ctypes.c_int),
     "fwigb_cnn_wgrad_partials": ([_V, _V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _V, _V],
                                  ctypes.c_int),
     "fwigb_cnn_reduce_partials": ([_V, ctypes.c_int, ctypes.c_int, _V, _V], ctypes.c_int),

@@ -9,8 +9,13 @@
 // the FWI workloads are). Channel counts are padded to 16 or 32; padded
 // channels carry zeros.
 //
-// Kernels (one 32 z x 8 x pixel tile per block):
-//   k_conv3x3      y = epilogue(conv(x, W) + b): GELU with the pre-activation
+// Kernels:
+//   k_conv3x3_tc   the 32-output-channel convolutions on the 5th-generation
+//                  tensor cores: tcgen05.mma (kind::f16, BF16 in, FP32 out)
+//                  with the accumulators in tensor memory, one 128-depth x
+//                  4-column pixel tile per block (see its comment)
+//   k_conv3x3      (one 32 z x 8 x pixel tile per block, warp-level
+//                  mma.sync) y = epilogue(conv(x, W) + b): GELU with the pre-activation
 //                  kept (forward), linear FP32 (last layer), or linear times
 //                  GELU'(z) (backward data, where W is the flipped,
 //                  transposed kernel: dX = conv(dZ, W'))
@@ -161,6 +166,232 @@ __global__ void __launch_bounds__(256) k_conv3x3(const __nv_bfloat16* __restrict
         }
       }
     }
+}
+
+// ---------------------------------------------------------------------------
+// tcgen05 convolution (sm_100 family). The convolution is an implicit GEMM
+// per output column: D[128 depths][32 couts] = sum over 9 taps of
+// A_tap[128][CIN] * B_tap[CIN][32]. Both operands live in shared memory in the
+// canonical no-swizzle K-major layout: 16-byte units of 8 consecutive
+// channels, 8-row core matrices 128 bytes apart (SBO) and channel groups LBO
+// apart. Rows of the input tile are consecutive depths of one column, so the
+// operand of a tap (ky, kx) is the tile column x + kx started ky rows down: a
+// descriptor offset of 16 ky bytes. One thread issues the MMAs; the FP32
+// accumulators (4 columns x 32 couts = 128 TMEM columns) are read back by
+// the block's four warps with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31,
+// i.e. depths z0 + 32w + lane) and go through the fused epilogue.
+constexpr int kTcRows = 128, kTcCols = 4;  // pixels per block: 128 depths x 4 columns
+constexpr int kTcTileRows = kTcRows + 2, kTcTileCols = kTcCols + 2;
+constexpr unsigned long long kTcWaitNs = 2000000000ull;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init1(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait (global timer) for phase `parity` of an mbarrier.
+__device__ __forceinline__ bool mbar_wait_ns(uint64_t* bar, unsigned parity) {
+  const unsigned long long t0 = global_ns();
+  for (unsigned n = 0;; ++n) {
+    if (mbar_test(bar, parity)) return true;
+    if ((n & 255u) == 255u && global_ns() - t0 > kTcWaitNs) return false;
+  }
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: start, leading (K-direction) and stride
+// (8-row-group) byte offsets, all >> 4; descriptor version 1; no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t start, uint32_t lbo, uint32_t sbo) {
+  return static_cast<uint64_t>((start >> 4) & 0x3FFFu) | (static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16) |
+         (static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major,
+// N = 32, M = 128.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(kTcIdesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
+  unsigned r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// CIN in {16, 32} input channels, 32 output channels. EPI kEpiGelu (bias,
+// pre-activation and GELU, BF16) or kEpiDGelu (times GELU'(z_prev), BF16).
+// wpack: the B operand in its shared-memory layout, 16-byte units (q, n) at
+// (q * 32 + n) for q = tap * CIN/8 + channel group (k_pack_weights_tc).
+template <int CIN, int EPI>
+__global__ void __launch_bounds__(128) k_conv3x3_tc(const __nv_bfloat16* __restrict__ x_in, int Hz, int Wx,
+                                                    const uint4* __restrict__ wpack,
+                                                    const float* __restrict__ bias, __nv_bfloat16* __restrict__ y,
+                                                    __nv_bfloat16* __restrict__ z_pre,
+                                                    const __nv_bfloat16* __restrict__ z_prev, unsigned* err) {
+  constexpr int QA = CIN / 8;                                    // channel groups of the input
+  constexpr int A_UNITS = QA * kTcTileCols * kTcTileRows;        // 16-byte units of the input tile
+  constexpr uint32_t LBO_A = kTcTileCols * kTcTileRows * 16;     // between channel groups
+  constexpr int QB = 9 * CIN / 8;                                // channel groups of B over the taps
+  constexpr uint32_t A_BYTES = A_UNITS * 16;
+  extern __shared__ __align__(128) uint8_t tc_smem[];
+  uint4* sA = reinterpret_cast<uint4*>(tc_smem);
+  uint4* sB = reinterpret_cast<uint4*>(tc_smem + A_BYTES);
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  const int z0 = blockIdx.x * kTcRows, x0 = blockIdx.y * kTcCols;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(&tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  for (int u = tid; u < A_UNITS; u += blockDim.x) {
+    const int q = u % QA, rest = u / QA;
+    const int r = rest % kTcTileRows, c = rest / kTcTileRows;
+    const int z = z0 + r - 1, x = x0 + c - 1;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (z >= 0 && z < Hz && x >= 0 && x < Wx)
+      v = *reinterpret_cast<const uint4*>(x_in + (static_cast<size_t>(x) * Hz + z) * CIN + q * 8);
+    sA[(q * kTcTileCols + c) * kTcTileRows + r] = v;
+  }
+  for (int u = tid; u < QB * 32; u += blockDim.x) sB[u] = wpack[u];
+  if (tid == 0) mbar_init1(&mbar);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // operands visible to the tensor cores
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  if (tid == 0) {
+    const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+#pragma unroll 1
+    for (int j = 0; j < kTcCols; ++j)
+#pragma unroll 1
+      for (int tap = 0; tap < 9; ++tap) {
+        const int ky = tap / 3, kx = tap % 3;
+#pragma unroll
+        for (int s = 0; s < CIN / 16; ++s) {
+          const uint32_t a = a0 + ((2 * s * kTcTileCols + (j + kx)) * kTcTileRows + ky) * 16;
+          const uint32_t b = b0 + (tap * QA + 2 * s) * 32 * 16;
+          tc_mma(tmem + j * 32, smem_desc(a, LBO_A, 128), smem_desc(b, 32 * 16, 128), (tap | s) != 0);
+        }
+      }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(&mbar))
+                 : "memory");
+  }
+  bool ok = mbar_wait_ns(&mbar, 0);
+  if (!ok) {
+    atomicOr(err, 2u);
+    mbar_wait_ns(&mbar, 0);  // let MMAs in flight finish before the memory goes away
+  }
+  ok = __all_sync(0xffffffffu, ok);
+  tc_fence_after();
+  if (ok) {
+#pragma unroll 1
+    for (int j = 0; j < kTcCols; ++j) {
+      float v[32];
+      tc_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + j * 32, v);
+      const int z = z0 + warp * 32 + lane, x = x0 + j;
+      if (z < Hz && x < Wx) {
+        const size_t p = (static_cast<size_t>(x) * Hz + z) * 32;
+        unsigned o0[16], o1[16];
+        if (EPI == kEpiGelu) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const float a = v[2 * c] + bias[2 * c], b = v[2 * c + 1] + bias[2 * c + 1];
+            o0[c] = pack_bf16(a, b);
+            o1[c] = pack_bf16(gelu(a), gelu(b));
+          }
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            reinterpret_cast<uint4*>(z_pre + p)[k] = make_uint4(o0[4 * k], o0[4 * k + 1], o0[4 * k + 2], o0[4 * k + 3]);
+            reinterpret_cast<uint4*>(y + p)[k] = make_uint4(o1[4 * k], o1[4 * k + 1], o1[4 * k + 2], o1[4 * k + 3]);
+          }
+        } else {
+          const uint4* zp = reinterpret_cast<const uint4*>(z_prev + p);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const uint4 w = zp[k];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const unsigned h = e == 0 ? w.x : (e == 1 ? w.y : (e == 2 ? w.z : w.w));
+              // BF16 -> FP32 is exact: the BF16 bits are the top half of the float.
+              const float lo = __uint_as_float(h << 16), hi = __uint_as_float(h & 0xFFFF0000u);
+              const int c = 4 * k + e;
+              o0[c] = pack_bf16(v[2 * c] * gelu_grad(lo), v[2 * c + 1] * gelu_grad(hi));
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            reinterpret_cast<uint4*>(y + p)[k] = make_uint4(o0[4 * k], o0[4 * k + 1], o0[4 * k + 2], o0[4 * k + 3]);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
+}
+
+// Packs W[9][cin][cout] (FP32) into the B operand of k_conv3x3_tc: unit
+// (q, n) of 8 BF16 = B[n][k = 8q .. 8q+7] with B[n][tap*KIN + kk] =
+// W[tap][kk][n] (forward, KIN = cin_pad) or W[8 - tap][n][kk] (transposed:
+// the data gradient, KIN = cout_pad, n over cin_pad). N must be 32.
+__global__ void k_pack_weights_tc(const float* __restrict__ w, int cin, int cout, int CIN, int COUT, int transposed,
+                                  uint4* __restrict__ out) {
+  const int KIN = transposed ? COUT : CIN;
+  const int total = 9 * KIN / 8 * 32;
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= total) return;
+  const int n = u % 32, q = u / 32;
+  unsigned h[4];
+  for (int e2 = 0; e2 < 4; ++e2) {
+    float v[2];
+    for (int t = 0; t < 2; ++t) {
+      const int k = q * 8 + e2 * 2 + t, tap = k / KIN, kk = k % KIN;
+      int ci, co, tp;
+      if (transposed) {
+        ci = n;
+        co = kk;
+        tp = 8 - tap;
+      } else {
+        ci = kk;
+        co = n;
+        tp = tap;
+      }
+      v[t] = (ci < cin && co < cout) ? w[(static_cast<size_t>(tp) * cin + ci) * cout + co] : 0.0f;
+    }
+    h[e2] = pack_bf16(v[0], v[1]);
+  }
+  out[u] = make_uint4(h[0], h[1], h[2], h[3]);
 }
 
 // Weight gradient partials. One block (9 warps, warp = tap) per 32 x 8 pixel
@@ -404,6 +635,48 @@ int fwigb_cnn_wgrad_partials(const void* x, const void* dz, int Hz, int Wx, int 
 }
 
 int fwigb_cnn_tile_count(int Hz, int Wx) { return (Hz / kTz) * ((Wx + kTx - 1) / kTx); }
+
+int fwigb_cnn_conv3x3_tc(const void* x, int Hz, int Wx, int cin_pad, int epilogue, const void* wpack,
+                         const float* bias, void* y_bf16, void* z_pre, const void* z_prev, unsigned* err_word,
+                         void* stream) {
+  if (!x || !wpack || !y_bf16 || !err_word || Hz <= 0 || Wx <= 0) return FWIGB_ERR_ARG;
+  if (epilogue == kEpiGelu && (!bias || !z_pre)) return FWIGB_ERR_ARG;
+  if (epilogue == kEpiDGelu && !z_prev) return FWIGB_ERR_ARG;
+  if (epilogue != kEpiGelu && epilogue != kEpiDGelu) return FWIGB_ERR_UNSUPPORTED;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const dim3 grid((Hz + kTcRows - 1) / kTcRows, (Wx + kTcCols - 1) / kTcCols);
+  const auto* xi = static_cast<const __nv_bfloat16*>(x);
+  const auto* wp = static_cast<const uint4*>(wpack);
+  auto* yo = static_cast<__nv_bfloat16*>(y_bf16);
+  auto* zo = static_cast<__nv_bfloat16*>(z_pre);
+  const auto* zi = static_cast<const __nv_bfloat16*>(z_prev);
+  auto launch = [&](auto kernel, int cin) -> cudaError_t {
+    const size_t smem = static_cast<size_t>(cin / 8) * kTcTileCols * kTcTileRows * 16 + 9 * cin / 8 * 32 * 16;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    kernel<<<grid, 128, smem, s>>>(xi, Hz, Wx, wp, bias, yo, zo, zi, err_word);
+    return cudaGetLastError();
+  };
+  cudaError_t e;
+  if (cin_pad == 16)
+    e = epilogue == kEpiGelu ? launch(k_conv3x3_tc<16, kEpiGelu>, 16) : launch(k_conv3x3_tc<16, kEpiDGelu>, 16);
+  else if (cin_pad == 32)
+    e = epilogue == kEpiGelu ? launch(k_conv3x3_tc<32, kEpiGelu>, 32) : launch(k_conv3x3_tc<32, kEpiDGelu>, 32);
+  else
+    return FWIGB_ERR_UNSUPPORTED;
+  return e == cudaSuccess ? FWIGB_OK : FWIGB_ERR_CUDA;
+}
+
+int fwigb_cnn_pack_weights_tc(const float* w, int cin, int cout, int cin_pad, int cout_pad, int transposed,
+                              void* pack, void* stream) {
+  if (!w || !pack || cin <= 0 || cout <= 0 || cin > cin_pad || cout > cout_pad) return FWIGB_ERR_ARG;
+  const int kin = transposed ? cout_pad : cin_pad, nout = transposed ? cin_pad : cout_pad;
+  if ((kin != 16 && kin != 32) || nout != 32) return FWIGB_ERR_UNSUPPORTED;
+  const int total = 9 * kin / 8 * 32;
+  k_pack_weights_tc<<<(total + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      w, cin, cout, cin_pad, cout_pad, transposed, static_cast<uint4*>(pack));
+  return cudaGetLastError() == cudaSuccess ? FWIGB_OK : FWIGB_ERR_CUDA;
+}
 
 int fwigb_cnn_reduce_partials(const float* partials, int nblocks, int n, float* out, void* stream) {
   if (!partials || !out || nblocks <= 0 || n <= 0) return FWIGB_ERR_ARG;

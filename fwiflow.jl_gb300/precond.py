@@ -15,7 +15,11 @@ g * gain directly lets the bright cells dominate.
 Every arithmetic step of the network runs in the library's own sm_103a
 kernels (csrc/cnn.cu: BF16 tensor-core convolutions with FP32 accumulation,
 weight gradients, masked MSE, Adam); torch tensors only hold the device
-memory, and the torch current stream is the one the kernels run on.
+memory, and the torch current stream is the one the kernels run on. With
+use_tc (the default) the convolutions with 32 outputs -- the first five
+layers and every data gradient -- run on tcgen05 (tensor memory
+accumulators); the 3-output head and the weight gradients on warp-level
+mma.sync.
 
 Image layout of the kernels: pixel p = x * Hz + z (z fastest), channels
 innermost; a model-shaped array (nz, nx) maps to it by transposition.
@@ -92,8 +96,9 @@ class CnnPreconditioner:
     # (real in, real out, padded in, padded out) per layer
     LAYERS = [(N_IN, WIDTH, 16, 32)] + [(WIDTH, WIDTH, 32, 32)] * (DEPTH - 2) + [(WIDTH, N_OUT, 32, 16)]
 
-    def __init__(self, Hz: int, Wx: int, seed: int = 0, device: int = 0):
+    def __init__(self, Hz: int, Wx: int, seed: int = 0, device: int = 0, use_tc: bool = True):
         torch = _torch()
+        self.use_tc = use_tc
         if Hz % 32:
             raise ValueError("Hz must be a multiple of 32")
         self.Hz, self.Wx, self.npix = Hz, Wx, Hz * Wx
@@ -129,6 +134,12 @@ class CnnPreconditioner:
         self.lpart = torch.zeros((self.npix + 255) // 256, **f32)
         self.target = torch.zeros((self.npix, N_OUT), **f32)
         self.mask = torch.zeros(self.npix, **f32)
+        # tcgen05 operand packs: forward (layers with 32 outputs) and data gradient (layers 1..)
+        self.tc = [torch.empty(9 * cip // 8 * 32 * 4, dtype=torch.int32, device=self.dev) if cop == 32 else None
+                   for (_, _, cip, cop) in self.LAYERS]
+        self.tc_t = [torch.empty(9 * cop // 8 * 32 * 4, dtype=torch.int32, device=self.dev) if k > 0 else None
+                     for k, (_, _, cip, cop) in enumerate(self.LAYERS)]
+        self.err = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self.step = 0
         self.pack()
 
@@ -167,6 +178,12 @@ class CnnPreconditioner:
             if self.frag_t[k] is not None:
                 self._ck(self.lib.fwigb_cnn_pack_weights(self._p(self.W[k]), cip, cop, cip, cop, 1,
                                                          self._p(self.frag_t[k]), s))
+            if self.tc[k] is not None:
+                self._ck(self.lib.fwigb_cnn_pack_weights_tc(self._p(self.W[k]), cip, cop, cip, cop, 0,
+                                                            self._p(self.tc[k]), s))
+            if self.tc_t[k] is not None:
+                self._ck(self.lib.fwigb_cnn_pack_weights_tc(self._p(self.W[k]), cip, cop, cip, cop, 1,
+                                                            self._p(self.tc_t[k]), s))
 
     # -- network
     def forward(self, x_dev=None):
@@ -176,9 +193,15 @@ class CnnPreconditioner:
         x = self.x0 if x_dev is None else x_dev
         for k, (_, _, cip, cop) in enumerate(self.LAYERS):
             if k < DEPTH - 1:
-                self._ck(self.lib.fwigb_cnn_conv3x3(self._p(x), self.Hz, self.Wx, cip, cop, EPI_GELU,
-                                                    self._p(self.frag[k]), self._p(self.b[k]), self._p(self.y[k]),
-                                                    None, self._p(self.z[k]), None, s))
+                if self.use_tc:
+                    self._ck(self.lib.fwigb_cnn_conv3x3_tc(self._p(x), self.Hz, self.Wx, cip, EPI_GELU,
+                                                           self._p(self.tc[k]), self._p(self.b[k]),
+                                                           self._p(self.y[k]), self._p(self.z[k]), None,
+                                                           self._p(self.err), s))
+                else:
+                    self._ck(self.lib.fwigb_cnn_conv3x3(self._p(x), self.Hz, self.Wx, cip, cop, EPI_GELU,
+                                                        self._p(self.frag[k]), self._p(self.b[k]),
+                                                        self._p(self.y[k]), None, self._p(self.z[k]), None, s))
                 x = self.y[k]
             else:
                 self._ck(self.lib.fwigb_cnn_conv3x3(self._p(x), self.Hz, self.Wx, cip, cop, EPI_LINEAR_F32,
@@ -203,9 +226,14 @@ class CnnPreconditioner:
             nb = (self.npix + self.chunk - 1) // self.chunk
             self._ck(self.lib.fwigb_cnn_reduce_partials(self._p(self.bpart), nb, cop, self._p(self.gb[k]), s))
             if k > 0:  # data gradient through the previous layer's GELU
-                self._ck(self.lib.fwigb_cnn_conv3x3(self._p(dz), self.Hz, self.Wx, cop, cip, EPI_DGELU,
-                                                    self._p(self.frag_t[k]), None, self._p(self.dz[k - 1]), None,
-                                                    None, self._p(self.z[k - 1]), s))
+                if self.use_tc:
+                    self._ck(self.lib.fwigb_cnn_conv3x3_tc(self._p(dz), self.Hz, self.Wx, cop, EPI_DGELU,
+                                                           self._p(self.tc_t[k]), None, self._p(self.dz[k - 1]),
+                                                           None, self._p(self.z[k - 1]), self._p(self.err), s))
+                else:
+                    self._ck(self.lib.fwigb_cnn_conv3x3(self._p(dz), self.Hz, self.Wx, cop, cip, EPI_DGELU,
+                                                        self._p(self.frag_t[k]), None, self._p(self.dz[k - 1]),
+                                                        None, None, self._p(self.z[k - 1]), s))
                 dz = self.dz[k - 1]
 
     def adam(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8) -> None:
@@ -280,6 +308,10 @@ class CnnPreconditioner:
     def state(self) -> dict:
         return {f"W{k}": self.W[k].cpu().numpy() for k in range(DEPTH)} | \
                {f"b{k}": self.b[k].cpu().numpy() for k in range(DEPTH)}
+
+    def tc_error(self) -> int:
+        """Error bits the tcgen05 kernels raised (bit 1: a bounded wait gave up)."""
+        return int(self.err.item())
 
     def load_state(self, st: dict) -> None:
         torch = _torch()

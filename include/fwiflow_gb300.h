@@ -216,6 +216,20 @@ const char *fwigb_noalloc_last_error(void);
 int fwigb_cnn_conv3x3(const void *x, int Hz, int Wx, int cin_pad, int cout_pad, int epilogue, const void *wfrag,
                       const float *bias, void *y_bf16, float *y_f32, void *z_pre, const void *z_prev,
                       void *stream);
+/* The convolutions with 32 outputs on the 5th-generation tensor cores
+ * (tcgen05.mma, accumulators in tensor memory; 128 x 4 pixels per block):
+ * cin_pad in {16, 32}, epilogue 0 (GELU, with z_pre) or 2 (times GELU'(z_prev)),
+ * wpack from fwigb_cnn_pack_weights_tc. A block whose bounded wait for its
+ * MMAs gives up sets bit 1 of *err_word (device memory) and writes nothing.
+ * Any Hz > 0. */
+int fwigb_cnn_conv3x3_tc(const void *x, int Hz, int Wx, int cin_pad, int epilogue, const void *wpack,
+                         const float *bias, void *y_bf16, void *z_pre, const void *z_prev, unsigned *err_word,
+                         void *stream);
+/* Packs FP32 weights W[9][cin][cout] into the tcgen05 B operand of a
+ * convolution with 32 outputs (cout_pad = 32), or (transposed != 0) of its
+ * data gradient (cin_pad = 32 outputs, cout_pad in {16, 32} inputs). */
+int fwigb_cnn_pack_weights_tc(const float *w, int cin, int cout, int cin_pad, int cout_pad, int transposed,
+                              void *pack, void *stream);
 /* Number of 32 x 8 pixel tiles (blocks) of an Hz x Wx image. */
 int fwigb_cnn_tile_count(int Hz, int Wx);
 /* Per-tile partial weight gradients [tiles][9][cin_pad][cout_pad] (FP32) of

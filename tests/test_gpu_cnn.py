@@ -110,3 +110,36 @@ def test_training_reduces_the_loss(gpu_lib, fw):
     net.train(samples, epochs=40, lr=2e-3)
     after = net.evaluate(samples)
     assert after < 0.5 * before, (before, after)
+
+
+def test_tcgen05_convolutions_match_mma_sync(gpu_lib, fw):
+    """The tcgen05 convolutions (tensor-memory accumulators) against the
+    warp-level mma.sync ones, which match PyTorch above: same weights and
+    input, every layer's pre-activation / activation and every data gradient
+    (BF16, 1e-2), the FP32 output (1e-3); no kernel raised its error bit.
+    The image height (96) is not a multiple of the 128-depth tcgen05 tile."""
+    import torch
+    from fwiflow_gb300.precond import CnnPreconditioner
+
+    Hz, Wx = 96, 37
+    a = CnnPreconditioner(Hz, Wx, seed=5, use_tc=True)
+    b = CnnPreconditioner(Hz, Wx, seed=5, use_tc=False)
+    torch.manual_seed(1)
+    x = torch.randn(5, Hz, Wx).numpy()
+    t = torch.randn(3, Hz, Wx).numpy()
+    m = np.ones((Hz, Wx))
+    for net in (a, b):
+        net.stage(x, t, m)
+        out = net.forward()
+        net.loss_and_grad(out)
+        net.backward(net.dz[-1])
+    torch.cuda.synchronize()
+    assert a.tc_error() == 0
+    for k in range(len(a.z)):
+        assert rel(a.z[k].float().cpu(), b.z[k].float().cpu()) < 1e-2, ("z", k)
+        assert rel(a.y[k].float().cpu(), b.y[k].float().cpu()) < 1e-2, ("y", k)
+    assert rel(a.out.cpu(), b.out.cpu()) < 1e-3
+    for k in range(len(a.dz) - 1):
+        assert rel(a.dz[k].float().cpu(), b.dz[k].float().cpu()) < 1e-2, ("dz", k)
+    for k in range(len(a.gW)):
+        assert rel(a.gW[k].cpu(), b.gW[k].cpu()) < 1e-2, ("dW", k)
