@@ -178,8 +178,9 @@ __global__ void __launch_bounds__(256) k_conv3x3(const __nv_bfloat16* __restrict
 // operand of a tap (ky, kx) is the tile column x + kx started ky rows down: a
 // descriptor offset of 16 ky bytes. One thread issues the MMAs; the FP32
 // accumulators (4 columns x 32 couts = 128 TMEM columns) are read back by
-// the block's four warps with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31,
-// i.e. depths z0 + 32w + lane) and go through the fused epilogue.
+// the block's two warpgroups with tcgen05.ld (warp w owns TMEM lanes
+// 32 (w % 4) .. +31, i.e. depths z0 + 32 (w % 4) + lane; warpgroup g takes
+// columns 2g and 2g + 1) and go through the fused epilogue.
 constexpr int kTcRows = 128, kTcCols = 4;  // pixels per block: 128 depths x 4 columns
 constexpr int kTcTileRows = kTcRows + 2, kTcTileCols = kTcCols + 2;
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
@@ -251,7 +252,7 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
 // wpack: the B operand in its shared-memory layout, 16-byte units (q, n) at
 // (q * 32 + n) for q = tap * CIN/8 + channel group (k_pack_weights_tc).
 template <int CIN, int EPI>
-__global__ void __launch_bounds__(128) k_conv3x3_tc(const __nv_bfloat16* __restrict__ x_in, int Hz, int Wx,
+__global__ void __launch_bounds__(256) k_conv3x3_tc(const __nv_bfloat16* __restrict__ x_in, int Hz, int Wx,
                                                     const uint4* __restrict__ wpack,
                                                     const float* __restrict__ bias, __nv_bfloat16* __restrict__ y,
                                                     __nv_bfloat16* __restrict__ z_pre,
@@ -315,11 +316,12 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(const __nv_bfloat16* __restr
   ok = __all_sync(0xffffffffu, ok);
   tc_fence_after();
   if (ok) {
+    const int quarter = warp & 3, wg = warp >> 2;
 #pragma unroll 1
-    for (int j = 0; j < kTcCols; ++j) {
+    for (int j = 2 * wg; j < 2 * wg + 2; ++j) {
       float v[32];
-      tc_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + j * 32, v);
-      const int z = z0 + warp * 32 + lane, x = x0 + j;
+      tc_ld32(tmem + (static_cast<uint32_t>(quarter * 32) << 16) + j * 32, v);
+      const int z = z0 + quarter * 32 + lane, x = x0 + j;
       if (z < Hz && x < Wx) {
         const size_t p = (static_cast<size_t>(x) * Hz + z) * 32;
         unsigned o0[16], o1[16];
@@ -654,7 +656,7 @@ int fwigb_cnn_conv3x3_tc(const void* x, int Hz, int Wx, int cin_pad, int epilogu
     const size_t smem = static_cast<size_t>(cin / 8) * kTcTileCols * kTcTileRows * 16 + 9 * cin / 8 * 32 * 16;
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    kernel<<<grid, 128, smem, s>>>(xi, Hz, Wx, wp, bias, yo, zo, zi, err_word);
+    kernel<<<grid, 256, smem, s>>>(xi, Hz, Wx, wp, bias, yo, zo, zi, err_word);
     return cudaGetLastError();
   };
   cudaError_t e;

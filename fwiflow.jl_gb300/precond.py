@@ -319,3 +319,39 @@ class CnnPreconditioner:
             self.W[k].copy_(torch.from_numpy(np.asarray(st[f"W{k}"], dtype=np.float32)))
             self.b[k].copy_(torch.from_numpy(np.asarray(st[f"b{k}"], dtype=np.float32)))
         self.pack()
+
+
+def benchmark_convs(Hz: int = 352, Wx: int = 832, reps: int = 50, device: int = 0) -> dict:
+    """Tensor throughput of the 32 -> 32 channel convolution (forward, GELU)
+    on one Hz x Wx image: tcgen05 and warp-level mma.sync kernels, CUDA
+    events on the current stream, 2 * 9 * 32 * 32 flops per pixel."""
+    torch = _torch()
+    net = CnnPreconditioner(Hz, Wx, seed=0, device=device)
+    x = torch.randn(net.npix, 32, device=net.dev).to(torch.bfloat16)
+    y = torch.empty_like(x)
+    z = torch.empty_like(x)
+    s = net._s()
+    flops = 2.0 * 9 * 32 * 32 * net.npix
+    out = {"image": [Hz, Wx], "flops_per_call": flops}
+    for name in ("tcgen05", "mma_sync"):
+        def call():
+            if name == "tcgen05":
+                net._ck(net.lib.fwigb_cnn_conv3x3_tc(x.data_ptr(), Hz, Wx, 32, EPI_GELU, net.tc[1].data_ptr(),
+                                                     net.b[1].data_ptr(), y.data_ptr(), z.data_ptr(), None,
+                                                     net.err.data_ptr(), s))
+            else:
+                net._ck(net.lib.fwigb_cnn_conv3x3(x.data_ptr(), Hz, Wx, 32, 32, EPI_GELU, net.frag[1].data_ptr(),
+                                                  net.b[1].data_ptr(), y.data_ptr(), None, z.data_ptr(), None, s))
+        for _ in range(5):
+            call()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        us = e0.elapsed_time(e1) * 1e3 / reps
+        out[name] = {"us_per_call": us, "tflops": flops / us / 1e6}
+    out["tc_error"] = net.tc_error()
+    return out
+
