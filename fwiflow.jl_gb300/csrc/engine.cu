@@ -418,6 +418,12 @@ struct fwigb_ctx {
   // Launch extents per pack.
   std::vector<SweepGrid> pack_grid;
   int last_groups = 0;
+  // CUDA graph of a lone-shot group's whole launch sequence, replayed while
+  // everything it was captured from is unchanged (graph_key).
+  bool use_graphs = true;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<uint64_t> graph_key;
+  long long graph_launches = 0;
   bool illum = false;       // accumulate the source illumination in the runs
   bool illum_valid = false; // the last run accumulated it
   bool model_set = false;
@@ -1094,62 +1100,115 @@ int run(fwigb_ctx* ctx, int calc_id) {
       while (a > 0 && nst[a - 1] - 2 < step) --a;
       return a;
     };
-    // Fresh wavefields and gathers for every member (libCUFD.cu:163-187).
-    CK(cudaMemsetAsync(ctx->g_fields.p, 0, static_cast<size_t>(G) * ctx->fields_stride * sizeof(float), s));
-    for (int k = 0; k < G; ++k) {
-      const ShotPlan& pl = ctx->plans[mem[k]];
-      const size_t per = static_cast<size_t>(pl.nrec) * pl.nSteps;
-      CK(cudaMemsetAsync(ctx->shot_data.as<float>(pl.data_off + per), 0, per * sizeof(float), s));
-      if (adj) CK(cudaMemsetAsync(ctx->shot_gstf.as<float>(pl.gstf_off), 0, pl.nSteps * sizeof(float), s));
-    }
-    if (adj || ctx->illum)
-      CK(cudaMemsetAsync(ctx->g_grads.p, 0, static_cast<size_t>(G) * ctx->grads_stride * sizeof(float), s));
-    const int ntop = nst[0];
-    for (int it = 0; it <= ntop - 2; ++it) {
-      const int a = active(it);
-      TIMED(0, launches += launch_sweep(ctx, 0, ctx->tx[0], ctx->rows[0], a, it, adj, d_err));
-      TIMED(1, launches += launch_sweep(ctx, 1, ctx->tx[1], ctx->rows[1], a, 0, false, d_err));
-    }
-    if (if_res) {
+    long long group_launches = 0;
+    // The group's launch sequence (eager, or recorded into a CUDA graph).
+    auto enqueue = [&]() -> int {
+      // Fresh wavefields and gathers for every member (libCUFD.cu:163-187).
+      CK(cudaMemsetAsync(ctx->g_fields.p, 0, static_cast<size_t>(G) * ctx->fields_stride * sizeof(float), s));
       for (int k = 0; k < G; ++k) {
         const ShotPlan& pl = ctx->plans[mem[k]];
-        const int nt = pl.nSteps;
-        const size_t per = static_cast<size_t>(pl.nrec) * nt;
-        const float* tw = ctx->shot_taper.as<float>(pl.taper_off);
-        const float* to = tw;
-        const float* tr = ctx->per_trace_taper ? tw + per : tw + nt;
-        const int nb = residual_blocks(pl.nrec * nt);
-        launch_residual(s, pl.nrec, nt, ctx->shot_data.as<float>(pl.data_off),
-                        ctx->shot_data.as<float>(pl.data_off + per), ctx->shot_data.as<float>(pl.data_off + 2 * per),
-                        to, tr, ctx->per_trace_taper ? 1 : 0, ctx->partials.as<double>());
-        launch_sum_partials(s, ctx->partials.as<double>(), nb, d_misfit);
-        launches += 2;
+        const size_t per = static_cast<size_t>(pl.nrec) * pl.nSteps;
+        CK(cudaMemsetAsync(ctx->shot_data.as<float>(pl.data_off + per), 0, per * sizeof(float), s));
+        if (adj) CK(cudaMemsetAsync(ctx->shot_gstf.as<float>(pl.gstf_off), 0, pl.nSteps * sizeof(float), s));
       }
-    }
-    if (adj) {
-      // Zero the adjoint fields and the 8 memory arrays (libCUFD.cu:337-351):
-      // field slots 5..17 of every member.
-      for (int k = 0; k < G; ++k) {
-        const size_t n = static_cast<size_t>(ctx->geo.ldz) * ctx->plans[mem[k]].nx;
-        CK(cudaMemsetAsync(ctx->g_fields.as<float>(k * ctx->fields_stride + 5 * n), 0, 13 * n * sizeof(float), s));
+      if (adj || ctx->illum)
+        CK(cudaMemsetAsync(ctx->g_grads.p, 0, static_cast<size_t>(G) * ctx->grads_stride * sizeof(float), s));
+      const int ntop = nst[0];
+      for (int it = 0; it <= ntop - 2; ++it) {
+        const int a = active(it);
+        TIMED(0, group_launches += launch_sweep(ctx, 0, ctx->tx[0], ctx->rows[0], a, it, adj, d_err));
+        TIMED(1, group_launches += launch_sweep(ctx, 1, ctx->tx[1], ctx->rows[1], a, 0, false, d_err));
       }
-      // The reference's first el_velocity_adj acts on all-zero fields (no-op);
-      // then res_injection(nSteps-1) + el_stress_adj, source_grad(nSteps-2),
-      // reverse velocity of step nSteps-2 ... (libCUFD.cu:353-445), with
-      // backward iteration j meaning step nSteps_k - 2 - j of member k.
-      TIMED(3, launches += launch_sweep(ctx, 3, ctx->tx[3], 1, G, -1, false, d_err));
-      for (int j = 0; j <= ntop - 2; ++j) {
-        const int a = active(j);
-        TIMED(2, launches += launch_sweep(ctx, 2, ctx->tx[2], 1, a, j, false, d_err));
-        TIMED(3, launches += launch_sweep(ctx, 3, ctx->tx[3], 1, a, j, false, d_err));
+      if (if_res) {
+        for (int k = 0; k < G; ++k) {
+          const ShotPlan& pl = ctx->plans[mem[k]];
+          const int nt = pl.nSteps;
+          const size_t per = static_cast<size_t>(pl.nrec) * nt;
+          const float* tw = ctx->shot_taper.as<float>(pl.taper_off);
+          const float* to = tw;
+          const float* tr = ctx->per_trace_taper ? tw + per : tw + nt;
+          const int nb = residual_blocks(pl.nrec * nt);
+          launch_residual(s, pl.nrec, nt, ctx->shot_data.as<float>(pl.data_off),
+                          ctx->shot_data.as<float>(pl.data_off + per), ctx->shot_data.as<float>(pl.data_off + 2 * per),
+                          to, tr, ctx->per_trace_taper ? 1 : 0, ctx->partials.as<double>());
+          launch_sum_partials(s, ctx->partials.as<double>(), nb, d_misfit);
+          group_launches += 2;
+        }
       }
+      if (adj) {
+        // Zero the adjoint fields and the 8 memory arrays (libCUFD.cu:337-351):
+        // field slots 5..17 of every member.
+        for (int k = 0; k < G; ++k) {
+          const size_t n = static_cast<size_t>(ctx->geo.ldz) * ctx->plans[mem[k]].nx;
+          CK(cudaMemsetAsync(ctx->g_fields.as<float>(k * ctx->fields_stride + 5 * n), 0, 13 * n * sizeof(float), s));
+        }
+        // The reference's first el_velocity_adj acts on all-zero fields (no-op);
+        // then res_injection(nSteps-1) + el_stress_adj, source_grad(nSteps-2),
+        // reverse velocity of step nSteps-2 ... (libCUFD.cu:353-445), with
+        // backward iteration j meaning step nSteps_k - 2 - j of member k.
+        TIMED(3, group_launches += launch_sweep(ctx, 3, ctx->tx[3], 1, G, -1, false, d_err));
+        for (int j = 0; j <= ntop - 2; ++j) {
+          const int a = active(j);
+          TIMED(2, group_launches += launch_sweep(ctx, 2, ctx->tx[2], 1, a, j, false, d_err));
+          TIMED(3, group_launches += launch_sweep(ctx, 3, ctx->tx[3], 1, a, j, false, d_err));
+        }
+      }
+      if (adj || ctx->illum) {
+        float* gb = ctx->grads.as<float>();
+        launch_reduce_grads(s, nz, ctx->p.nx, ctx->geo.ldz, G, slots, adj ? gb : nullptr, gb + ctx->cells,
+                            gb + 2 * ctx->cells, ctx->illum ? gb + 3 * ctx->cells : nullptr);
+        ++group_launches;
+      }
+      return FWIGB_OK;
+    };
+    if (ctx->use_graphs && !ctx->timing && G == 1) {
+      // A lone shot: its ~4 launches per time step are replayed from a CUDA
+      // graph captured on first use. The key holds every value the captured
+      // launches depend on: the parameter packs (pointers, geometry, TMA
+      // maps), tile choices, flags and the buffers of the memsets / residual.
+      std::vector<uint64_t> key = {static_cast<uint64_t>(calc_id), static_cast<uint64_t>(ctx->illum),
+                                   static_cast<uint64_t>(ctx->per_trace_taper)};
+      for (int k = 0; k < 4; ++k) key.push_back((static_cast<uint64_t>(ctx->tx[k]) << 8) | ctx->rows[k]);
+      const ShotPlan& pl0 = ctx->plans[mem[0]];
+      for (uint64_t v : {static_cast<uint64_t>(pl0.nrec), static_cast<uint64_t>(pl0.nSteps),
+                         static_cast<uint64_t>(pl0.nx), static_cast<uint64_t>(pl0.data_off),
+                         static_cast<uint64_t>(pl0.gstf_off), static_cast<uint64_t>(pl0.taper_off),
+                         static_cast<uint64_t>(ctx->fields_stride), static_cast<uint64_t>(ctx->grads_stride),
+                         reinterpret_cast<uint64_t>(ctx->g_fields.p), reinterpret_cast<uint64_t>(ctx->g_grads.p),
+                         reinterpret_cast<uint64_t>(ctx->shot_data.p), reinterpret_cast<uint64_t>(ctx->shot_gstf.p),
+                         reinterpret_cast<uint64_t>(ctx->shot_taper.p), reinterpret_cast<uint64_t>(ctx->partials.p),
+                         reinterpret_cast<uint64_t>(ctx->grads.p), reinterpret_cast<uint64_t>(ctx->scal.p),
+                         reinterpret_cast<uint64_t>(ctx->g_slots.p)})
+        key.push_back(v);
+      const size_t pack_words = ctx->pack1.size() * sizeof(SweepPack<1>) / sizeof(uint64_t);
+      const uint64_t* pw = reinterpret_cast<const uint64_t*>(ctx->pack1.data());
+      key.insert(key.end(), pw, pw + pack_words);
+      if (!ctx->graph_exec || key != ctx->graph_key) {
+        if (ctx->graph_exec) {
+          cudaGraphExecDestroy(ctx->graph_exec);
+          ctx->graph_exec = nullptr;
+        }
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue();
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(s, &graph);
+        if (rc != FWIGB_OK) {
+          if (graph) cudaGraphDestroy(graph);
+          return rc;
+        }
+        CK(ec);
+        const cudaError_t ei = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        CK(ei);
+        ctx->graph_key = std::move(key);
+        ctx->graph_launches = group_launches;
+      }
+      group_launches = ctx->graph_launches;
+      CK(cudaGraphLaunch(ctx->graph_exec, s));
+    } else {
+      TRY_RC(enqueue());
     }
-    if (adj || ctx->illum) {
-      float* gb = ctx->grads.as<float>();
-      launch_reduce_grads(s, nz, ctx->p.nx, ctx->geo.ldz, G, slots, adj ? gb : nullptr, gb + ctx->cells,
-                          gb + 2 * ctx->cells, ctx->illum ? gb + 3 * ctx->cells : nullptr);
-      ++launches;
-    }
+    launches += group_launches;
     // The next group reuses the slots and maps; wait for this one.
     if (gi + 1 < groups.size()) CK(cudaStreamSynchronize(s));
   }
@@ -1310,6 +1369,7 @@ int fwigb_destroy(fwigb_ctx* ctx) {
                     &ctx->g_slots})
     b->release();
   for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return FWIGB_OK;
@@ -1387,6 +1447,18 @@ long long fwigb_last_launch_count(const fwigb_ctx* ctx) { return ctx ? ctx->laun
 int fwigb_tile_config(const fwigb_ctx* ctx, int* tile_x) {
   if (!ctx || !tile_x) return FWIGB_ERR_ARG;
   for (int k = 0; k < 4; ++k) tile_x[k] = ctx->tx[k];
+  return FWIGB_OK;
+}
+
+int fwigb_set_graphs(fwigb_ctx* ctx, int enable) {
+  if (!ctx) return FWIGB_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->use_graphs = enable != 0;
+  if (!ctx->use_graphs && ctx->graph_exec) {
+    cudaGraphExecDestroy(ctx->graph_exec);
+    ctx->graph_exec = nullptr;
+    ctx->graph_key.clear();
+  }
   return FWIGB_OK;
 }
 

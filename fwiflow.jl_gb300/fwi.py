@@ -217,6 +217,10 @@ class FwiContext:
         t = None if widths is None else np.ascontiguousarray(widths, dtype=np.int32)
         _lib.check(self._lib.fwigb_set_tile_config(self._h, _lib.iptr(t)), self._h)
 
+    def set_graphs(self, enable: bool) -> None:
+        """Replay a lone shot's launch sequence from a CUDA graph (default on)."""
+        _lib.check(self._lib.fwigb_set_graphs(self._h, int(enable)), self._h)
+
     def set_kernel_timing(self, enable: bool) -> None:
         _lib.check(self._lib.fwigb_set_kernel_timing(self._h, int(enable)), self._h)
 

@@ -172,6 +172,13 @@ int fwigb_tile_config(const fwigb_ctx *ctx, int *tile_x);
 int fwigb_set_tile_config(fwigb_ctx *ctx, const int *tile_x);
 int fwigb_tile_rows(const fwigb_ctx *ctx, int *rows);
 
+/* CUDA graphs (on by default): a run whose shots form one group of one shot
+ * records its whole launch sequence (about 4 launches per time step) into a
+ * CUDA graph the first time and replays it while the staged shot, the model
+ * and data buffers and the tile choices are unchanged; per-kernel timing
+ * runs eagerly. enable = 0 runs every call eagerly. */
+int fwigb_set_graphs(fwigb_ctx *ctx, int enable);
+
 /* Per-kernel timing of fwigb_run: when enabled, a CUDA event pair on the
  * context's stream brackets every sweep launch. Kinds: 0 forward stress,
  * 1 forward velocity, 2 backward sweep B, 3 backward sweep C. */
