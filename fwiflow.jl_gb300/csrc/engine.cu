@@ -1161,9 +1161,10 @@ int run(fwigb_ctx* ctx, int calc_id) {
       }
       return FWIGB_OK;
     };
-    if (ctx->use_graphs && !ctx->timing && G == 1) {
+    if (ctx->use_graphs && !ctx->timing && G == 1 && groups.size() == 1) {
       // A lone shot: its ~4 launches per time step are replayed from a CUDA
-      // graph captured on first use. The key holds every value the captured
+      // graph captured on first use (a call of several groups would record a
+      // graph per group and call, so it runs eagerly). The key holds every value the captured
       // launches depend on: the parameter packs (pointers, geometry, TMA
       // maps), tile choices, flags and the buffers of the memsets / residual.
       std::vector<uint64_t> key = {static_cast<uint64_t>(calc_id), static_cast<uint64_t>(ctx->illum),
@@ -1447,6 +1448,42 @@ long long fwigb_last_launch_count(const fwigb_ctx* ctx) { return ctx ? ctx->laun
 int fwigb_tile_config(const fwigb_ctx* ctx, int* tile_x) {
   if (!ctx || !tile_x) return FWIGB_ERR_ARG;
   for (int k = 0; k < 4; ++k) tile_x[k] = ctx->tx[k];
+  return FWIGB_OK;
+}
+
+int fwigb_sweep_time(fwigb_ctx* ctx, int kind, int reps, double* us_per_launch) {
+  if (!ctx || !us_per_launch || kind < 0 || kind > 3 || reps < 1) return FWIGB_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (ctx->group_size < 1) {
+    ctx->err = "no group has run yet";
+    return FWIGB_ERR_ARG;
+  }
+  cudaStream_t s = ctx->stream;
+  unsigned* d_err = reinterpret_cast<unsigned*>(ctx->scal.as<char>() + 16);
+  const int rows = kind < 2 ? ctx->rows[kind] : 1;
+  CK(cudaStreamSynchronize(s));
+  CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  for (int r = 0; r < reps; ++r) launch_sweep(ctx, kind, ctx->tx[kind], rows, ctx->group_size, 0, false, d_err);
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamEndCapture(s, &graph));
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  CK(ei);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaGraphLaunch(exec, s));  // warm-up
+  CK(cudaEventRecord(e0, s));
+  CK(cudaGraphLaunch(exec, s));
+  CK(cudaEventRecord(e1, s));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0.0f;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaGraphExecDestroy(exec);
+  *us_per_launch = 1e3 * ms / reps;
   return FWIGB_OK;
 }
 

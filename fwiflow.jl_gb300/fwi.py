@@ -221,6 +221,13 @@ class FwiContext:
         """Replay a lone shot's launch sequence from a CUDA graph (default on)."""
         _lib.check(self._lib.fwigb_set_graphs(self._h, int(enable)), self._h)
 
+    def sweep_time(self, kind: int, reps: int = 50) -> float:
+        """Microseconds per launch of sweep `kind` (0 F1, 1 F2, 2 B, 3 C) on
+        the last run's group, from a CUDA graph of back-to-back launches."""
+        out = np.zeros(1)
+        _lib.check(self._lib.fwigb_sweep_time(self._h, int(kind), int(reps), _lib.dptr(out)), self._h)
+        return float(out[0])
+
     def set_kernel_timing(self, enable: bool) -> None:
         _lib.check(self._lib.fwigb_set_kernel_timing(self._h, int(enable)), self._h)
 

@@ -172,12 +172,19 @@ int fwigb_tile_config(const fwigb_ctx *ctx, int *tile_x);
 int fwigb_set_tile_config(fwigb_ctx *ctx, const int *tile_x);
 int fwigb_tile_rows(const fwigb_ctx *ctx, int *rows);
 
-/* CUDA graphs (on by default): a run whose shots form one group of one shot
- * records its whole launch sequence (about 4 launches per time step) into a
+/* CUDA graphs (on by default): a run whose shots form a single group of one
+ * shot records its whole launch sequence (about 4 launches per time step) into a
  * CUDA graph the first time and replays it while the staged shot, the model
  * and data buffers and the tile choices are unchanged; per-kernel timing
  * runs eagerly. enable = 0 runs every call eagerly. */
 int fwigb_set_graphs(fwigb_ctx *ctx, int enable);
+
+/* Average duration of one launch of sweep `kind` (0 forward stress, 1 forward
+ * velocity, 2 backward B, 3 backward C) over the last run's (last) group, at
+ * its tuned tile: `reps` back-to-back launches recorded in a CUDA graph and
+ * timed with events around the graph (no per-launch event overhead). The
+ * launches work on the live wavefields, which the next run resets. */
+int fwigb_sweep_time(fwigb_ctx *ctx, int kind, int reps, double *us_per_launch);
 
 /* Per-kernel timing of fwigb_run: when enabled, a CUDA event pair on the
  * context's stream brackets every sweep launch. Kinds: 0 forward stress,
