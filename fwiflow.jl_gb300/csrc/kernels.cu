@@ -22,6 +22,7 @@
 #include <cudaTypedefs.h>
 
 #include <cstdint>
+#include <utility>
 
 namespace fwigb {
 namespace {
@@ -149,16 +150,23 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
 // (32, TX): lane threadIdx.x covers R adjacent depths (R = TZ / 32),
 // threadIdx.y the column; `b` is the index of its first cell in a staged box
 // (column stride BOXZ = TZ + 8).
+// Programmatic dependent launch: a sweep lets the next sweep's blocks be
+// scheduled as soon as all of its own blocks have started, and waits for the
+// previous sweep to complete (and its writes to be visible) before it
+// touches any field. The parameter reads and tile classification before the
+// wait overlap the previous sweep's last blocks.
 #define SWEEP_KERNEL_TILE(TZ_)                                                 \
   const int shot = K == 1 ? 0 : static_cast<int>(blockIdx.z);                  \
   const Geo& g0 = P.slots[shot].g;                                             \
   const int z0 = blockIdx.x * (TZ_), x0 = blockIdx.y * TX;                     \
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");              \
   if (z0 >= g0.nz || x0 >= g0.nx) return;                                      \
   const TileSplit ts = tile_split(g0, TX, (TZ_));                              \
   const bool fast = static_cast<int>(blockIdx.x) >= ts.ftz0 &&                 \
                     static_cast<int>(blockIdx.x) < ts.ftz1 &&                  \
                     static_cast<int>(blockIdx.y) >= ts.ftx0 &&                 \
-                    static_cast<int>(blockIdx.y) < ts.ftx1;
+                    static_cast<int>(blockIdx.y) < ts.ftx1;                    \
+  asm volatile("griddepcontrol.wait;" ::: "memory");
 
 #define SWEEP_BODY_SLOT()                                                      \
   const ShotSlot& S = P.slots[shot];                                           \
@@ -1109,6 +1117,24 @@ constexpr size_t smem_bytes(int na) {
     }                              \
   }
 
+// Launches a sweep with programmatic stream serialisation (see
+// SWEEP_KERNEL_TILE); inside a stream capture this becomes a programmatic
+// dependency edge of the graph.
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 dim3 sweep_grid(int tx, int tz, const SweepGrid& gr, int nshots) {
   return dim3((gr.nz + tz - 1) / tz, (gr.nx + tx - 1) / tx, nshots);
 }
@@ -1116,12 +1142,13 @@ dim3 sweep_grid(int tx, int tz, const SweepGrid& gr, int nshots) {
 template <int K>
 int launch_fwd_stress(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int it,
                       bool save, unsigned* err) {
+  const int sv = save ? 1 : 0;
   if (rows == 2)
-    FWIGB_DISPATCH_TX(tx, k_fwd_stress<TX, K, 2><<<sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
-                                                   smem_bytes<TX, kBoxZFwd>(2), s>>>(p, it, save ? 1 : 0, err))
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_stress<TX, K, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
+                                     smem_bytes<TX, kBoxZFwd>(2), s, p, it, sv, err))
   else
-    FWIGB_DISPATCH_TX(tx, k_fwd_stress<TX, K, 1><<<sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
-                                                   smem_bytes<TX, kBoxZ>(2), s>>>(p, it, save ? 1 : 0, err))
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_stress<TX, K, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+                                     smem_bytes<TX, kBoxZ>(2), s, p, it, sv, err))
   return 1;
 }
 
@@ -1129,27 +1156,27 @@ template <int K>
 int launch_fwd_velocity(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
                         unsigned* err) {
   if (rows == 2)
-    FWIGB_DISPATCH_TX(tx, k_fwd_velocity<TX, K, 2><<<sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
-                                                     smem_bytes<TX, kBoxZFwd>(3), s>>>(p, err))
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_velocity<TX, K, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
+                                     smem_bytes<TX, kBoxZFwd>(3), s, p, err))
   else
-    FWIGB_DISPATCH_TX(tx, k_fwd_velocity<TX, K, 1><<<sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
-                                                     smem_bytes<TX, kBoxZ>(3), s>>>(p, err))
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_velocity<TX, K, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+                                     smem_bytes<TX, kBoxZ>(3), s, p, err))
   return 1;
 }
 
 template <int K>
 int launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, k_bwd_B<TX, K><<<sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX), smem_bytes<TX, kBoxZ>(5), s>>>(p, j,
-                                                                                                         err))
+  FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+                                   smem_bytes<TX, kBoxZ>(5), s, p, j, err))
   return 1;
 }
 
 template <int K>
 int launch_bwd_C(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, k_bwd_C<TX, K><<<sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX), smem_bytes<TX, kBoxZ>(5), s>>>(p, j,
-                                                                                                         err))
+  FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, K>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+                                   smem_bytes<TX, kBoxZ>(5), s, p, j, err))
   return 1;
 }
 
