@@ -555,6 +555,8 @@ struct oracle_para {
   int nz, nx, nSteps, nPml, nPad;
   float dz, dx, dt, f0;
   int if_win;
+  int if_filter;     // "filter" key present (Parameter.cpp:155-167)
+  float filter[4];   // band-pass corner frequencies f0 < f1 <= f2 < f3 [Hz]
 };
 
 struct oracle_shot {
@@ -574,6 +576,50 @@ enum { ORACLE_OK = 0, ORACLE_BAD_ARG = 1, ORACLE_COURANT = 3 };
 // [nrec][nSteps] (calc 0/1). syn_out[i] (optional) receives shot i's gathers as
 // the reference keeps them: raw for calc 2, after the taper for calc 0/1.
 // res_out[i] (optional) receives the adjoint source (tapered residual).
+// Band-pass of bp_filter1d (utilities.cu:872-923, cuda_bp_filter1d :596-626)
+// on each of nrec traces of nt samples: the trace zero-padded to 2 nt, its
+// spectrum times amp(f)^2 with amp the sin / 1 / cos band-pass of the corner
+// frequencies (bin frequencies k / (2 nt dt) in float, as the kernel computes
+// them), back to time, cropped to nt and scaled by 1 / (2 nt). Restated as
+// the equivalent circular convolution with the real, even impulse response
+// h[m] = (a_0 + 2 sum_{k=1}^{nt-1} a_k cos(pi k m / nt) + a_nt cos(pi m)) / (2 nt),
+// a_k = amp(f_k)^2, accumulated in double.
+static void bp_filter(float* data, int nt, int nrec, float dt, const float* fc) {
+  const int n2 = 2 * nt;
+  const float df = static_cast<float>(1.0 / dt / n2);
+  std::vector<double> a(nt + 1);
+  const double kPi = 3.14159265358979323846;
+  for (int k = 0; k <= nt; ++k) {
+    const float freq = k * df;
+    float amp;
+    if (freq >= fc[0] && freq < fc[1])
+      amp = static_cast<float>(std::sin(kPi / 2.0 * (freq - fc[0]) / (fc[1] - fc[0])));
+    else if (freq >= fc[1] && freq < fc[2])
+      amp = 1.0f;
+    else if (freq >= fc[2] && freq < fc[3])
+      amp = static_cast<float>(std::cos(kPi / 2.0 * (freq - fc[2]) / (fc[3] - fc[2])));
+    else
+      amp = 0.0f;
+    a[k] = static_cast<double>(amp * amp);
+  }
+  std::vector<double> h(n2);
+  for (int m = 0; m < n2; ++m) {
+    double s = a[0] + a[nt] * ((m & 1) ? -1.0 : 1.0);
+    for (int k = 1; k < nt; ++k) s += 2.0 * a[k] * std::cos(kPi * k * m / nt);
+    h[m] = s / n2;
+  }
+  std::vector<float> y(nt);
+  for (int r = 0; r < nrec; ++r) {
+    float* x = data + static_cast<size_t>(r) * nt;
+    for (int t = 0; t < nt; ++t) {
+      double acc = 0.0;
+      for (int s = 0; s < nt; ++s) acc += static_cast<double>(x[s]) * h[(t - s + n2) % n2];
+      y[t] = static_cast<float>(acc);
+    }
+    std::copy(y.begin(), y.end(), x);
+  }
+}
+
 static int cufd_impl(const oracle_para* p, const oracle_shot* shots, int group_size, const int* shot_ids,
                      const double* Lambda, const double* Mu, const double* Den, const double* stf, int calc_id,
                      const float* const* obs, float* const* syn_out, float* const* res_out, double* misfit,
@@ -707,6 +753,10 @@ static int cufd_impl(const oracle_para* p, const oracle_shot* shots, int group_s
       taper(o.data(), nSteps, nrec, g.dt, 0.005f);
       taper(data.data(), nSteps, nrec, g.dt, 0.005f);
     }
+    if (p->if_filter) {  // libCUFD.cu:273-277
+      bp_filter(o.data(), nSteps, nrec, g.dt, p->filter);
+      bp_filter(data.data(), nSteps, nrec, g.dt, p->filter);
+    }
     std::vector<float> res(data.size());
     for (int r = 0; r < nrec; ++r)
       for (int it = 0; it < nSteps; ++it) {
@@ -714,6 +764,7 @@ static int cufd_impl(const oracle_para* p, const oracle_shot* shots, int group_s
         res[k] = (it == 0) ? 0.0f : o[k] - data[k];
       }
     l2 += objective(res.data(), nrec * nSteps);
+    if (p->if_filter) bp_filter(res.data(), nSteps, nrec, g.dt, p->filter);  // libCUFD.cu:301-304
     if (p->if_win)
       taper_windowed(res.data(), nSteps, nrec, g.dt, 0.1f, sh.win_start, sh.win_end, sh.weights);
     else

@@ -36,7 +36,8 @@ REFHOST_LIB = os.path.join(HERE, "_ref", "librefhost_fwi.so")
 class _Para(ctypes.Structure):
     _fields_ = [("nz", ctypes.c_int), ("nx", ctypes.c_int), ("nSteps", ctypes.c_int), ("nPml", ctypes.c_int),
                 ("nPad", ctypes.c_int), ("dz", ctypes.c_float), ("dx", ctypes.c_float), ("dt", ctypes.c_float),
-                ("f0", ctypes.c_float), ("if_win", ctypes.c_int)]
+                ("f0", ctypes.c_float), ("if_win", ctypes.c_int), ("if_filter", ctypes.c_int),
+                ("filter", ctypes.c_float * 4)]
 
 
 class _Shot(ctypes.Structure):
@@ -132,7 +133,9 @@ def _iptr(a):
 def _run_group(p: dict, shots: list, ids: Sequence[int], nz: int, nx: int, nt: int, lam, mu, den, stf, calc_id: int,
                obs, nthreads: int, precision: str, illum: Optional[np.ndarray] = None):
     """One oracle_cufd call over shots sharing one grid and record length."""
-    para = _Para(nz, nx, nt, p["nPml"], p["nPad"], p["dz"], p["dx"], p["dt"], p["f0"], int(p["if_win"]))
+    fl = p.get("filter")
+    para = _Para(nz, nx, nt, p["nPml"], p["nPad"], p["dz"], p["dx"], p["dt"], p["f0"], int(p["if_win"]),
+                 int(fl is not None), (ctypes.c_float * 4)(*(fl if fl is not None else [0.0] * 4)))
     keep = []
     carr = (_Shot * len(shots))()
     for i, s in enumerate(shots):

@@ -7,12 +7,14 @@ parameter / survey / Data files written by the package's paraGen / surveyGen.
 Run from the repository root, where the reference sources are available:
 
     make -C oracle -f Makefile.refhost REF=/path/to/FwiFlow.jl
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]     (default: every case)
 
 Cases (all seeded, see fwiflow.jl_gb300/synthetic.py):
   tiny_elastic   32x48 interior, nPml 10, 200 steps, 2 shots: gathers, misfit, gradients
   tiny_acoustic  same geometry with Vs = 0 and constant density (the mu == 0 path)
   tiny_window    1 shot with per-trace windows and weights (if_win, utilities.cu:653-705)
+  tiny_filter    2 shots with the band-pass "filter" of the parameter file (bp_filter1d,
+                 utilities.cu:872-923, applied at libCUFD.cu:273-277 and 301-304)
   small_layered  the 100x200, 1000-step, 2-shot workload: misfit, norms and a strided
                  subsample of gathers and gradients
 """
@@ -37,7 +39,7 @@ OUT = os.path.dirname(os.path.abspath(__file__))
 STRIDE = 16
 
 
-def run_case(w, with_window=False):
+def run_case(w, with_window=False, para_extra=None):
     tmp = tempfile.mkdtemp()
     if with_window:
         rng = np.random.default_rng(7)
@@ -54,6 +56,11 @@ def run_case(w, with_window=False):
             f.write(json.dumps(p, separators=(",", ":")))
     else:
         para = w.write_files(tmp)
+    if para_extra:
+        p = json.load(open(para))
+        p.update(para_extra)
+        with open(para, "w") as f:
+            f.write(json.dumps(p, separators=(",", ":")))
     moduli = (lambda v: synthetic.tiny_moduli(w, v)) if w.name == "tiny" else w.moduli
     lo, mo, ro = moduli(w.vp_obs)
     lam, mu, rho = moduli(w.vp)
@@ -77,9 +84,21 @@ def save_full(name, w, r2, r0, r1, **meta):
     )
 
 
+FILTER = [3.0, 6.0, 14.0, 24.0]  # band-pass corners [Hz] of the tiny_filter case
+
+
 def main():
     if not orc.refhost_available():
         raise SystemExit("oracle/_ref/librefhost_fwi.so missing: build it with oracle/Makefile.refhost")
+    cases = set(sys.argv[1:]) or {"tiny_elastic", "tiny_acoustic", "tiny_window", "tiny_filter", "small_layered"}
+    if "tiny_filter" in cases:
+        kw = dict(nz=32, nx=48, nPml=10, nSteps=200, n_shots=2, seed=3)
+        w = synthetic.tiny(**kw)
+        _, r2, r0, r1 = run_case(w, para_extra={"filter": FILTER})
+        save_full("tiny_filter", w, r2, r0, r1, builder="tiny", filter=FILTER, kwargs=kw)
+    if not cases & {"tiny_elastic", "tiny_acoustic", "tiny_window", "small_layered"}:
+        print("golden fixtures written to", OUT)
+        return
     w = synthetic.tiny(nz=32, nx=48, nPml=10, nSteps=200, n_shots=2, seed=0)
     _, r2, r0, r1 = run_case(w)
     save_full("tiny_elastic", w, r2, r0, r1, builder="tiny", kwargs=dict(nz=32, nx=48, nPml=10, nSteps=200,

@@ -13,10 +13,13 @@ import pytest
 
 from conftest import golden_workload, rel
 
-TINY = ["tiny_elastic", "tiny_acoustic", "tiny_window"]
+TINY = ["tiny_elastic", "tiny_acoustic", "tiny_window", "tiny_filter"]
 # Oracle vs reference: both are float programs with the same operation order
 # except the mu / rho scatter (atomicAdd in the reference, a gather here).
 TOL_EXACT = 1e-6
+# The band-pass filter: the reference transforms with (emulated) cuFFT, the
+# oracle convolves with the same filter's impulse response in double.
+TOL = {"tiny_filter": 1e-5}
 
 
 @pytest.mark.parametrize("name", TINY)
@@ -24,14 +27,15 @@ def test_oracle_matches_golden(name, orc, tmp_path, fw):
     d, w, para, moduli = golden_workload(name, tmp_path)
     ids = list(range(len(w.shots)))
     lo, mo, ro = moduli(w.vp_obs)
+    tol = TOL.get(name, TOL_EXACT)
     r2 = orc.cufd(2, lo, mo, ro, w.stf, ids, para, write_files=True, want_gathers=True)
-    assert rel(np.stack(r2["gathers"]), d["gathers"]) < TOL_EXACT
+    assert rel(np.stack(r2["gathers"]), d["gathers"]) < tol
     lam, mu, rho = moduli(w.vp)
     r0 = orc.cufd(0, lam, mu, rho, w.stf, ids, para)
-    assert abs(r0["misfit"] - float(d["misfit"])) <= 1e-6 * abs(float(d["misfit"]))
+    assert abs(r0["misfit"] - float(d["misfit"])) <= tol * abs(float(d["misfit"]))
     r1 = orc.cufd(1, lam, mu, rho, w.stf, ids, para)
     for k in ("g_lambda", "g_mu", "g_den", "g_stf"):
-        assert rel(r1[k], d[k]) < TOL_EXACT, k
+        assert rel(r1[k], d[k]) < tol, k
 
 
 def test_oracle_matches_golden_small_layered(orc, tmp_path, fw):
