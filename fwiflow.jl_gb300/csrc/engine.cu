@@ -282,6 +282,43 @@ static void cpml_profile(int N, int len, int nPml, float dh, float f0, float dt,
   }
 }
 
+// Impulse response of bp_filter1d (utilities.cu:872-923 with the gains of
+// cuda_bp_filter1d, :596-626) for traces of nt samples: zero padding to 2 nt,
+// spectrum times amp(f)^2 (amp the sin / 1 / cos band-pass of the corners, bin
+// frequencies k / (2 nt dt) in float as the kernel computes them), inverse
+// transform and the 1 / (2 nt) normalisation make the filter a circular
+// convolution with h[m] = (a_0 + 2 sum_{0<k<nt} a_k cos(pi k m / nt) +
+// a_nt cos(pi m)) / (2 nt), a_k = amp(f_k)^2; only bins inside the band
+// contribute.
+static std::vector<float> bandpass_response(int nt, float dt, const float* fc) {
+  const int n2 = 2 * nt;
+  const float df = static_cast<float>(1.0 / dt / n2);
+  std::vector<std::pair<int, double>> a;
+  for (int k = 0; k <= nt; ++k) {
+    const float freq = k * df;
+    float amp;
+    if (freq >= fc[0] && freq < fc[1])
+      amp = static_cast<float>(std::sin(kPI / 2.0 * (freq - fc[0]) / (fc[1] - fc[0])));
+    else if (freq >= fc[1] && freq < fc[2])
+      amp = 1.0f;
+    else if (freq >= fc[2] && freq < fc[3])
+      amp = static_cast<float>(std::cos(kPI / 2.0 * (freq - fc[2]) / (fc[3] - fc[2])));
+    else
+      amp = 0.0f;
+    if (amp != 0.0f) a.emplace_back(k, static_cast<double>(amp * amp));
+  }
+  std::vector<float> h(n2, 0.0f);
+  for (int m = 0; m < n2; ++m) {
+    double v = 0.0;
+    for (const auto& [k, ak] : a) {
+      const double w = (k == 0 || k == nt) ? 1.0 : 2.0;
+      v += w * ak * std::cos(kPI * static_cast<double>(k) * m / nt);
+    }
+    h[m] = static_cast<float>(v / n2);
+  }
+  return h;
+}
+
 // sin^2 / cos^2 taper weights of cuda_window without windows (utilities.cu:707-747).
 static bool taper_weights(int nt, float dt, float ratio, float* w) {
   const float t0 = 0.0f, t3 = nt * dt, off = nt * dt * ratio;
@@ -370,6 +407,7 @@ struct ShotPlan {
   size_t blk_off = 0;   // ints: nbin + 1 + nrec (receiver bins, CSR)
   size_t data_off = 0;  // floats: obs | syn | res, each nrec * nSteps
   size_t taper_off = 0; // floats: 2 * nSteps, or 2 * nrec * nSteps with per-trace windows
+  size_t filt_off = 0;  // floats: the band-pass impulse response (2 * nSteps), when filtering
   size_t gstf_off = 0;  // floats: nSteps
   size_t cpmlx_off = 0; // floats: 6 * nx (CPML x profiles of the sub-grid)
   int rbz0 = 0, rbz1 = 0, rbx0 = 0, rbx1 = 0;  // receivers + source bounding box
@@ -397,6 +435,8 @@ struct fwigb_ctx {
   // Staged shots and their data.
   std::vector<ShotPlan> plans;
   DevBuf shot_src, shot_rec, shot_blk, shot_data, shot_taper, shot_gstf, shot_cpmlx;
+  DevBuf shot_filt, filt_tmp;  // band-pass impulse responses; two trace-block scratch buffers
+  size_t filt_tmp_floats = 0;
   bool with_obs = false;
   bool per_trace_taper = false;
   int nSteps_max = 0;  // longest staged record
@@ -652,8 +692,8 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
     ctx->err = "stf / shot_ids missing";
     return FWIGB_ERR_ARG;
   }
-  if (p.if_filter || p.if_src_update) {
-    ctx->err = "parameter file asks for the band-pass filter or source update, which this build does not implement";
+  if (p.if_src_update) {
+    ctx->err = "parameter file asks for the source update, which this build does not implement";
     return FWIGB_ERR_UNSUPPORTED;
   }
   CK(cudaSetDevice(ctx->device));
@@ -695,6 +735,22 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
     pl.cpmlx_off = n_cpmlx;
     n_cpmlx += 6 * static_cast<size_t>(pl.nx);
     ctx->plans.push_back(pl);
+  }
+  // Band-pass impulse responses, one per distinct record length.
+  std::vector<float> hfilt;
+  size_t tmp_need = 0;
+  if (p.if_filter) {
+    std::map<int, size_t> at;
+    for (ShotPlan& pl : ctx->plans) {
+      tmp_need = std::max(tmp_need, static_cast<size_t>(pl.nrec) * pl.nSteps);
+      auto it = at.find(pl.nSteps);
+      if (it == at.end()) {
+        it = at.emplace(pl.nSteps, hfilt.size()).first;
+        const std::vector<float> h = bandpass_response(pl.nSteps, p.dt, p.filter);
+        hfilt.insert(hfilt.end(), h.begin(), h.end());
+      }
+      pl.filt_off = it->second;
+    }
   }
   std::vector<float> hsrc(n_src), htaper(n_taper, 1.0f), hcpml(n_cpmlx);
   std::vector<int> hrec(n_rec), hblk(n_blk, 0);
@@ -777,6 +833,12 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
   CK(cudaMemcpyAsync(ctx->shot_rec.p, hrec.data(), n_rec * sizeof(int), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(ctx->shot_blk.p, hblk.data(), n_blk * sizeof(int), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(ctx->shot_taper.p, htaper.data(), n_taper * sizeof(float), cudaMemcpyHostToDevice, s));
+  if (p.if_filter) {
+    CK(ctx->shot_filt.ensure(hfilt.size() * sizeof(float)));
+    CK(cudaMemcpyAsync(ctx->shot_filt.p, hfilt.data(), hfilt.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    CK(ctx->filt_tmp.ensure(2 * tmp_need * sizeof(float)));
+    ctx->filt_tmp_floats = tmp_need;
+  }
   CK(cudaMemcpyAsync(ctx->shot_cpmlx.p, hcpml.data(), n_cpmlx * sizeof(float), cudaMemcpyHostToDevice, s));
   ctx->with_obs = with_obs;
   if (with_obs) {
@@ -1128,11 +1190,32 @@ int run(fwigb_ctx* ctx, int calc_id) {
           const float* to = tw;
           const float* tr = ctx->per_trace_taper ? tw + per : tw + nt;
           const int nb = residual_blocks(pl.nrec * nt);
-          launch_residual(s, pl.nrec, nt, ctx->shot_data.as<float>(pl.data_off),
-                          ctx->shot_data.as<float>(pl.data_off + per), ctx->shot_data.as<float>(pl.data_off + 2 * per),
-                          to, tr, ctx->per_trace_taper ? 1 : 0, ctx->partials.as<double>());
-          launch_sum_partials(s, ctx->partials.as<double>(), nb, d_misfit);
-          group_launches += 2;
+          const int pt = ctx->per_trace_taper ? 1 : 0;
+          float* obs = ctx->shot_data.as<float>(pl.data_off);
+          float* syn = ctx->shot_data.as<float>(pl.data_off + per);
+          float* res = ctx->shot_data.as<float>(pl.data_off + 2 * per);
+          if (!ctx->p.if_filter) {
+            launch_residual(s, pl.nrec, nt, obs, syn, res, to, tr, pt, ctx->partials.as<double>());
+            launch_sum_partials(s, ctx->partials.as<double>(), nb, d_misfit);
+            group_launches += 2;
+          } else {
+            // Taper, band-pass obs and syn, residual and misfit, band-pass the
+            // residual, adjoint taper (libCUFD.cu:256-310). The filtered
+            // synthetic replaces the gathers, as in the reference.
+            float* ta = ctx->filt_tmp.as<float>();
+            float* tb = ctx->filt_tmp.as<float>(ctx->filt_tmp_floats);
+            const float* h = ctx->shot_filt.as<float>(pl.filt_off);
+            launch_apply_taper(s, pl.nrec, nt, obs, ta, to, pt);
+            launch_apply_taper(s, pl.nrec, nt, syn, syn, to, pt);
+            launch_trace_filter(s, pl.nrec, nt, ta, tb, h);
+            launch_trace_filter(s, pl.nrec, nt, syn, ta, h);
+            CK(cudaMemcpyAsync(syn, ta, per * sizeof(float), cudaMemcpyDeviceToDevice, s));
+            launch_residual(s, pl.nrec, nt, tb, syn, res, nullptr, nullptr, 0, ctx->partials.as<double>());
+            launch_sum_partials(s, ctx->partials.as<double>(), nb, d_misfit);
+            launch_trace_filter(s, pl.nrec, nt, res, ta, h);
+            launch_apply_taper(s, pl.nrec, nt, ta, res, tr, pt);
+            group_launches += 8;
+          }
         }
       }
       if (adj) {
@@ -1179,7 +1262,9 @@ int run(fwigb_ctx* ctx, int calc_id) {
                          reinterpret_cast<uint64_t>(ctx->shot_data.p), reinterpret_cast<uint64_t>(ctx->shot_gstf.p),
                          reinterpret_cast<uint64_t>(ctx->shot_taper.p), reinterpret_cast<uint64_t>(ctx->partials.p),
                          reinterpret_cast<uint64_t>(ctx->grads.p), reinterpret_cast<uint64_t>(ctx->scal.p),
-                         reinterpret_cast<uint64_t>(ctx->g_slots.p)})
+                         reinterpret_cast<uint64_t>(ctx->g_slots.p), reinterpret_cast<uint64_t>(ctx->shot_filt.p),
+                         reinterpret_cast<uint64_t>(ctx->filt_tmp.p), static_cast<uint64_t>(ctx->filt_tmp_floats),
+                         static_cast<uint64_t>(pl0.filt_off)})
         key.push_back(v);
       const size_t pack_words = ctx->pack1.size() * sizeof(SweepPack<1>) / sizeof(uint64_t);
       const uint64_t* pw = reinterpret_cast<const uint64_t*>(ctx->pack1.data());
@@ -1366,7 +1451,8 @@ int fwigb_destroy(fwigb_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->media, &ctx->stage, &ctx->cpml, &ctx->grads, &ctx->scal, &ctx->partials,
                     &ctx->shot_src, &ctx->shot_rec, &ctx->shot_blk, &ctx->shot_data, &ctx->shot_taper,
-                    &ctx->shot_gstf, &ctx->shot_cpmlx, &ctx->g_fields, &ctx->g_store, &ctx->g_grads,
+                    &ctx->shot_gstf, &ctx->shot_cpmlx, &ctx->shot_filt, &ctx->filt_tmp, &ctx->g_fields,
+                    &ctx->g_store, &ctx->g_grads,
                     &ctx->g_slots})
     b->release();
   for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);

@@ -218,6 +218,14 @@ int residual_blocks(int n);
 void launch_residual(cudaStream_t s, int nrec, int nSteps, const float* obs, float* syn, float* res,
                      const float* taper_o, const float* taper_r, int per_trace, double* partials);
 void launch_sum_partials(cudaStream_t s, const double* partials, int n, double* acc);
+// (taper_o / taper_r may be null: a weight of 1.)
+
+// out = in * taper (per_trace: [nrec][nSteps], else [nSteps]).
+void launch_apply_taper(cudaStream_t s, int nrec, int nSteps, const float* in, float* out, const float* taper,
+                        int per_trace);
+// Band-pass of nrec traces of nt samples: y = x circularly convolved with the
+// impulse response h (2 nt floats); x and y distinct.
+void launch_trace_filter(cudaStream_t s, int nrec, int nt, const float* x, float* y, const float* h);
 
 // Column-major float grid (stride ldz) -> row-major double.
 void launch_to_rowmajor(cudaStream_t s, int nz, int nx, int ldz, const float* src, double* dst, double scale);

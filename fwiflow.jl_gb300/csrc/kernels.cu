@@ -1024,8 +1024,8 @@ __global__ void __launch_bounds__(kResThreads)
   for (size_t k = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; k < n;
        k += static_cast<size_t>(gridDim.x) * blockDim.x) {
     const int t = static_cast<int>(k % nSteps);
-    const float wo = per_trace ? taper_o[k] : taper_o[t];
-    const float wr = per_trace ? taper_r[k] : taper_r[t];
+    const float wo = taper_o ? (per_trace ? taper_o[k] : taper_o[t]) : 1.0f;
+    const float wr = taper_r ? (per_trace ? taper_r[k] : taper_r[t]) : 1.0f;
     const float s = syn[k] * wo;
     const float o = obs[k] * wo;
     syn[k] = s;
@@ -1042,6 +1042,45 @@ __global__ void __launch_bounds__(kResThreads)
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (threadIdx.x == 0) partials[blockIdx.x] = v;
   }
+}
+
+// out = in * taper (taper [nrec][nSteps] when per_trace, else [nSteps]); in
+// may be out.
+__global__ void k_apply_taper(int nrec, int nSteps, const float* in, float* out, const float* __restrict__ taper,
+                              int per_trace) {
+  const size_t n = static_cast<size_t>(nrec) * nSteps;
+  for (size_t k = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; k < n;
+       k += static_cast<size_t>(gridDim.x) * blockDim.x)
+    out[k] = in[k] * (per_trace ? taper[k] : taper[k % nSteps]);
+}
+
+// Band-pass of every trace as a circular convolution with the filter's
+// impulse response h (length 2 nt, see the engine): y[r][t] =
+// sum_{s < nt} x[r][s] h[(t - s) mod 2 nt]. Block: trace blockIdx.y, outputs
+// t0 .. t0 + 255; the samples and the 511 taps a chunk of 256 samples needs
+// are staged in shared memory. x and y are distinct.
+constexpr int kFilt = 256;
+__global__ void __launch_bounds__(kFilt) k_trace_filter(int nt, const float* __restrict__ x, float* __restrict__ y,
+                                                        const float* __restrict__ h) {
+  __shared__ float xs[kFilt];
+  __shared__ float hs[2 * kFilt];
+  const int r = blockIdx.y, t0 = blockIdx.x * kFilt, tid = threadIdx.x, t = t0 + tid;
+  const int n2 = 2 * nt;
+  const float* xr = x + static_cast<size_t>(r) * nt;
+  float acc = 0.0f;
+  for (int s0 = 0; s0 < nt; s0 += kFilt) {
+    xs[tid] = (s0 + tid < nt) ? xr[s0 + tid] : 0.0f;
+    for (int j = tid; j < 2 * kFilt - 1; j += kFilt) {
+      int m = (t0 - s0 - (kFilt - 1) + j) % n2;
+      if (m < 0) m += n2;
+      hs[j] = h[m];
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int u = 0; u < kFilt; ++u) acc += xs[u] * hs[tid - u + kFilt - 1];
+    __syncthreads();
+  }
+  if (t < nt) y[static_cast<size_t>(r) * nt + t] = acc;
 }
 
 // Adds the per-shot gradients and / or illuminations of a shot group into
@@ -1262,6 +1301,15 @@ void launch_residual(cudaStream_t s, int nrec, int nSteps, const float* obs, flo
                      const float* taper_o, const float* taper_r, int per_trace, double* partials) {
   const int nb = residual_blocks(nrec * nSteps);
   k_residual<<<nb, kResThreads, 0, s>>>(nrec, nSteps, obs, syn, res, taper_o, taper_r, per_trace, partials);
+}
+
+void launch_apply_taper(cudaStream_t s, int nrec, int nSteps, const float* in, float* out, const float* taper,
+                        int per_trace) {
+  k_apply_taper<<<residual_blocks(nrec * nSteps), kResThreads, 0, s>>>(nrec, nSteps, in, out, taper, per_trace);
+}
+
+void launch_trace_filter(cudaStream_t s, int nrec, int nt, const float* x, float* y, const float* h) {
+  k_trace_filter<<<dim3((nt + kFilt - 1) / kFilt, nrec), kFilt, 0, s>>>(nt, x, y, h);
 }
 
 void launch_sum_partials(cudaStream_t s, const double* partials, int n, double* acc) {

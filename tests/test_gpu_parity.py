@@ -34,7 +34,7 @@ def fp32_floor(orc, w, para, moduli, ids, d):
     return out
 
 
-@pytest.mark.parametrize("name", ["tiny_elastic", "tiny_acoustic", "tiny_window"])
+@pytest.mark.parametrize("name", ["tiny_elastic", "tiny_acoustic", "tiny_window", "tiny_filter"])
 def test_cuda_matches_reference_golden(name, gpu_lib, fw, orc, tmp_path):
     """Tolerance: 1e-4 (data, misfit) / 1e-3 (gradients), or 4x the case's FP32
     floor where FP32 rounding alone already moves the reference further."""
