@@ -408,6 +408,7 @@ struct ShotPlan {
   size_t data_off = 0;  // floats: obs | syn | res, each nrec * nSteps
   size_t taper_off = 0; // floats: 2 * nSteps, or 2 * nrec * nSteps with per-trace windows
   size_t filt_off = 0;  // floats: the band-pass impulse response (2 * nSteps), when filtering
+  std::vector<float> src_amp;  // tapered source wavelet (host; kept for the scratch outputs)
   size_t gstf_off = 0;  // floats: nSteps
   size_t cpmlx_off = 0; // floats: 6 * nx (CPML x profiles of the sub-grid)
   int rbz0 = 0, rbz1 = 0, rbx0 = 0, rbx1 = 0;  // receivers + source bounding box
@@ -436,6 +437,7 @@ struct fwigb_ctx {
   std::vector<ShotPlan> plans;
   DevBuf shot_src, shot_rec, shot_blk, shot_data, shot_taper, shot_gstf, shot_cpmlx;
   DevBuf shot_filt, filt_tmp;  // band-pass impulse responses; two trace-block scratch buffers
+  DevBuf scratch_tmp;          // conditioned observed data of the scratch outputs
   size_t filt_tmp_floats = 0;
   bool with_obs = false;
   bool per_trace_taper = false;
@@ -776,8 +778,10 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
       return FWIGB_ERR_ARG;
     }
     const double* row = stf + static_cast<size_t>(pl.id) * nt_max;
+    pl.src_amp.assign(nt, 0.0f);
     for (int it = 0; it < nt; ++it) {
       const float amp = static_cast<float>(row[it]) * w[it];
+      pl.src_amp[it] = amp;
       hsrc[pl.src_off + it] = scale * amp * p.dt;
       hsrc[pl.src_off + nt + it] = static_cast<float>(3.0 * scale * amp * p.dt);
     }
@@ -1096,6 +1100,58 @@ int autotune(fwigb_ctx* ctx, int nshots, int nx_max, bool adj) {
   return FWIGB_OK;
 }
 
+// Scratch outputs of a gradient call (libCUFD.cu:493-511), when the
+// parameter file names scratch_dir_name: per shot, the injected residual
+// (Residual_Shot<id>.bin), the processed synthetic (Syn_Shot<id>.bin), the
+// conditioned observed data -- tapered and, with a filter, band-passed --
+// (CondObs_Shot<id>.bin), each [nrec][nSteps] float, and the source wavelet
+// used (src_updated<id>.bin, nSteps floats).
+int write_scratch(fwigb_ctx* ctx) {
+  const Params& p = ctx->p;
+  cudaStream_t s = ctx->stream;
+  size_t need = 0;
+  for (const ShotPlan& pl : ctx->plans) need = std::max(need, static_cast<size_t>(pl.nrec) * pl.nSteps);
+  CK(ctx->scratch_tmp.ensure(2 * need * sizeof(float)));
+  float* ta = ctx->scratch_tmp.as<float>();
+  float* tb = ctx->scratch_tmp.as<float>(need);
+  std::vector<float> h;
+  auto write = [&](const std::string& name, const float* data, size_t n) -> int {
+    const std::string fn = p.scratch_dir_name + "/" + name;
+    std::FILE* fp = std::fopen(fn.c_str(), "wb");
+    if (!fp || std::fwrite(data, sizeof(float), n, fp) != n) {
+      if (fp) std::fclose(fp);
+      ctx->err = "cannot write " + fn;
+      return FWIGB_ERR_IO;
+    }
+    std::fclose(fp);
+    return FWIGB_OK;
+  };
+  for (const ShotPlan& pl : ctx->plans) {
+    const int nt = pl.nSteps;
+    const size_t per = static_cast<size_t>(pl.nrec) * nt;
+    const float* tw = ctx->shot_taper.as<float>(pl.taper_off);
+    launch_apply_taper(s, pl.nrec, nt, ctx->shot_data.as<float>(pl.data_off), ta, tw, ctx->per_trace_taper ? 1 : 0);
+    const float* cond = ta;
+    if (p.if_filter) {
+      launch_trace_filter(s, pl.nrec, nt, ta, tb, ctx->shot_filt.as<float>(pl.filt_off));
+      cond = tb;
+    }
+    h.resize(3 * per);
+    CK(cudaMemcpyAsync(h.data(), ctx->shot_data.as<float>(pl.data_off + 2 * per), per * sizeof(float),
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h.data() + per, ctx->shot_data.as<float>(pl.data_off + per), per * sizeof(float),
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h.data() + 2 * per, cond, per * sizeof(float), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const std::string id = std::to_string(pl.id);
+    TRY_RC(write("Residual_Shot" + id + ".bin", h.data(), per));
+    TRY_RC(write("Syn_Shot" + id + ".bin", h.data() + per, per));
+    TRY_RC(write("CondObs_Shot" + id + ".bin", h.data() + 2 * per, per));
+    TRY_RC(write("src_updated" + id + ".bin", pl.src_amp.data(), nt));
+  }
+  return FWIGB_OK;
+}
+
 int run(fwigb_ctx* ctx, int calc_id) {
   if (calc_id < 0 || calc_id > 2) {
     ctx->err = "calc_id must be 0, 1 or 2";
@@ -1304,6 +1360,7 @@ int run(fwigb_ctx* ctx, int calc_id) {
   ctx->last_calc = calc_id;
   ctx->last_groups = static_cast<int>(groups.size());
   ctx->illum_valid = ctx->illum;
+  if (adj && ctx->p.if_save_scratch) TRY_RC(write_scratch(ctx));
   return FWIGB_OK;
 }
 
@@ -1451,7 +1508,8 @@ int fwigb_destroy(fwigb_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->media, &ctx->stage, &ctx->cpml, &ctx->grads, &ctx->scal, &ctx->partials,
                     &ctx->shot_src, &ctx->shot_rec, &ctx->shot_blk, &ctx->shot_data, &ctx->shot_taper,
-                    &ctx->shot_gstf, &ctx->shot_cpmlx, &ctx->shot_filt, &ctx->filt_tmp, &ctx->g_fields,
+                    &ctx->shot_gstf, &ctx->shot_cpmlx, &ctx->shot_filt, &ctx->filt_tmp, &ctx->scratch_tmp,
+                    &ctx->g_fields,
                     &ctx->g_store, &ctx->g_grads,
                     &ctx->g_slots})
     b->release();

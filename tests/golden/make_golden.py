@@ -15,6 +15,8 @@ Cases (all seeded, see fwiflow.jl_gb300/synthetic.py):
   tiny_window    1 shot with per-trace windows and weights (if_win, utilities.cu:653-705)
   tiny_filter    2 shots with the band-pass "filter" of the parameter file (bp_filter1d,
                  utilities.cu:872-923, applied at libCUFD.cu:273-277 and 301-304)
+  tiny_scratch   the tiny_filter case with a "scratch_dir_name": the scratch outputs of its
+                 gradient call (libCUFD.cu:493-511) per shot
   small_layered  the 100x200, 1000-step, 2-shot workload: misfit, norms and a strided
                  subsample of gathers and gradients
 """
@@ -90,7 +92,19 @@ FILTER = [3.0, 6.0, 14.0, 24.0]  # band-pass corners [Hz] of the tiny_filter cas
 def main():
     if not orc.refhost_available():
         raise SystemExit("oracle/_ref/librefhost_fwi.so missing: build it with oracle/Makefile.refhost")
-    cases = set(sys.argv[1:]) or {"tiny_elastic", "tiny_acoustic", "tiny_window", "tiny_filter", "small_layered"}
+    cases = set(sys.argv[1:]) or {"tiny_elastic", "tiny_acoustic", "tiny_window", "tiny_filter", "tiny_scratch",
+                                  "small_layered"}
+    if "tiny_scratch" in cases:
+        kw = dict(nz=32, nx=48, nPml=10, nSteps=200, n_shots=2, seed=3)
+        w = synthetic.tiny(**kw)
+        scratch = tempfile.mkdtemp()
+        run_case(w, para_extra={"filter": FILTER, "scratch_dir_name": scratch})
+        out = {}
+        for sid in range(len(w.shots)):
+            for name in ("Residual_Shot", "Syn_Shot", "CondObs_Shot", "src_updated"):
+                out[f"{name}{sid}"] = np.fromfile(os.path.join(scratch, f"{name}{sid}.bin"), dtype=np.float32)
+        np.savez_compressed(os.path.join(OUT, "tiny_scratch.npz"), **out,
+                            meta=json.dumps({"builder": "tiny", "filter": FILTER, "kwargs": kw}))
     if "tiny_filter" in cases:
         kw = dict(nz=32, nx=48, nPml=10, nSteps=200, n_shots=2, seed=3)
         w = synthetic.tiny(**kw)
