@@ -408,6 +408,7 @@ struct ShotPlan {
   size_t data_off = 0;  // floats: obs | syn | res, each nrec * nSteps
   size_t taper_off = 0; // floats: 2 * nSteps, or 2 * nrec * nSteps with per-trace windows
   size_t filt_off = 0;  // floats: the band-pass impulse response (2 * nSteps), when filtering
+  size_t supd_off = 0;  // floats: source update block (supd_floats), when if_src_update
   std::vector<float> src_amp;  // tapered source wavelet (host; kept for the scratch outputs)
   size_t gstf_off = 0;  // floats: nSteps
   size_t cpmlx_off = 0; // floats: 6 * nx (CPML x profiles of the sub-grid)
@@ -438,6 +439,10 @@ struct fwigb_ctx {
   DevBuf shot_src, shot_rec, shot_blk, shot_data, shot_taper, shot_gstf, shot_cpmlx;
   DevBuf shot_filt, filt_tmp;  // band-pass impulse responses; two trace-block scratch buffers
   DevBuf scratch_tmp;          // conditioned observed data of the scratch outputs
+  // Source-wavelet update: per-shot blocks (taper, wavelet, twiddles, updated
+  // wavelet and its reverse source terms) and per-call spectra partial sums,
+  // coefficients and impulse response (reused shot after shot).
+  DevBuf shot_supd, supd_part, supd_coef, supd_k;
   size_t filt_tmp_floats = 0;
   bool with_obs = false;
   bool per_trace_taper = false;
@@ -687,6 +692,23 @@ int set_model(fwigb_ctx* ctx, const double* lam, const double* mu, const double*
   return FWIGB_OK;
 }
 
+// Per-shot block of the source-wavelet update (floats, 16-byte multiple):
+// [w2: nt][wavelet: nt][twiddles (cos, sin)(2 pi k / 2 nt): 2 * 2 nt]
+// [updated wavelet: nt][its szz terms: nt][its sxx terms: nt].
+struct SupdLayout {
+  size_t w2, amp, tw, upd, szz, sxx, size;
+  explicit SupdLayout(int nt) {
+    const size_t n = static_cast<size_t>(nt);
+    w2 = 0;
+    amp = n;
+    tw = 2 * n;
+    upd = 6 * n;
+    szz = 7 * n;
+    sxx = 8 * n;
+    size = (9 * n + 3) / 4 * 4;
+  }
+};
+
 int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* shot_ids, int n_shots, bool with_obs,
                 const float* obs) {
   const Params& p = ctx->p;
@@ -694,14 +716,10 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
     ctx->err = "stf / shot_ids missing";
     return FWIGB_ERR_ARG;
   }
-  if (p.if_src_update) {
-    ctx->err = "parameter file asks for the source update, which this build does not implement";
-    return FWIGB_ERR_UNSUPPORTED;
-  }
   CK(cudaSetDevice(ctx->device));
   const int nt_max = p.nSteps, nrm = ctx->nrec_max;
   ctx->plans.clear();
-  size_t n_src = 0, n_rec = 0, n_blk = 0, n_data = 0, n_taper = 0, n_gstf = 0, n_cpmlx = 0;
+  size_t n_src = 0, n_rec = 0, n_blk = 0, n_data = 0, n_taper = 0, n_gstf = 0, n_cpmlx = 0, n_supd = 0;
   for (int k = 0; k < n_shots; ++k) {
     const int id = shot_ids[k];
     if (id < 0 || id >= static_cast<int>(ctx->survey.size()) || !ctx->survey[id].present) {
@@ -734,6 +752,14 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
     n_taper += 2 * static_cast<size_t>(pl.nSteps) * (p.if_win ? pl.nrec : 1);
     pl.gstf_off = n_gstf;
     n_gstf += static_cast<size_t>(pl.nSteps);
+    if (p.if_src_update) {
+      if (pl.nSteps > 32768) {  // f * t of the spectra stays below 2^32
+        ctx->err = "the source update takes records of at most 32768 steps";
+        return FWIGB_ERR_ARG;
+      }
+      pl.supd_off = n_supd;
+      n_supd += SupdLayout(pl.nSteps).size;
+    }
     pl.cpmlx_off = n_cpmlx;
     n_cpmlx += 6 * static_cast<size_t>(pl.nx);
     ctx->plans.push_back(pl);
@@ -741,10 +767,11 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
   // Band-pass impulse responses, one per distinct record length.
   std::vector<float> hfilt;
   size_t tmp_need = 0;
+  if (p.if_filter || p.if_src_update)
+    for (const ShotPlan& pl : ctx->plans) tmp_need = std::max(tmp_need, static_cast<size_t>(pl.nrec) * pl.nSteps);
   if (p.if_filter) {
     std::map<int, size_t> at;
     for (ShotPlan& pl : ctx->plans) {
-      tmp_need = std::max(tmp_need, static_cast<size_t>(pl.nrec) * pl.nSteps);
       auto it = at.find(pl.nSteps);
       if (it == at.end()) {
         it = at.emplace(pl.nSteps, hfilt.size()).first;
@@ -754,7 +781,7 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
       pl.filt_off = it->second;
     }
   }
-  std::vector<float> hsrc(n_src), htaper(n_taper, 1.0f), hcpml(n_cpmlx);
+  std::vector<float> hsrc(n_src), htaper(n_taper, 1.0f), hcpml(n_cpmlx), hsupd(n_supd, 0.0f);
   std::vector<int> hrec(n_rec), hblk(n_blk, 0);
   const float* zprof = nullptr;
   std::vector<float> zh(6 * p.nz);
@@ -784,6 +811,21 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
       pl.src_amp[it] = amp;
       hsrc[pl.src_off + it] = scale * amp * p.dt;
       hsrc[pl.src_off + nt + it] = static_cast<float>(3.0 * scale * amp * p.dt);
+    }
+    if (p.if_src_update) {
+      // Taper of the padded traces (cuda_window over 2 nt, ratio 0.01,
+      // utilities.cu:955-958), the wavelet and the transform's twiddles.
+      const SupdLayout L(nt);
+      float* b = hsupd.data() + pl.supd_off;
+      std::vector<float> w2(2 * static_cast<size_t>(nt));
+      taper_weights(2 * nt, p.dt, 0.01f, w2.data());
+      std::copy(w2.begin(), w2.begin() + nt, b + L.w2);
+      std::copy(pl.src_amp.begin(), pl.src_amp.end(), b + L.amp);
+      const double two_pi = 6.283185307179586476925286766559;
+      for (int k = 0; k < 2 * nt; ++k) {
+        b[L.tw + 2 * k] = static_cast<float>(std::cos(two_pi * k / (2.0 * nt)));
+        b[L.tw + 2 * k + 1] = static_cast<float>(std::sin(two_pi * k / (2.0 * nt)));
+      }
     }
     // Receivers (sub-grid coordinates) and their 32 x 8 bins.
     const ShotGeom& g = *pl.geom;
@@ -840,8 +882,22 @@ int stage_shots(fwigb_ctx* ctx, const double* stf, int n_stf_rows, const int* sh
   if (p.if_filter) {
     CK(ctx->shot_filt.ensure(hfilt.size() * sizeof(float)));
     CK(cudaMemcpyAsync(ctx->shot_filt.p, hfilt.data(), hfilt.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+  }
+  if (p.if_filter || p.if_src_update) {
     CK(ctx->filt_tmp.ensure(2 * tmp_need * sizeof(float)));
     ctx->filt_tmp_floats = tmp_need;
+  }
+  if (p.if_src_update) {
+    int nt_big = 1, nb_big = 1;
+    for (const ShotPlan& pl : ctx->plans) {
+      nt_big = std::max(nt_big, pl.nSteps);
+      nb_big = std::max(nb_big, src_spectra_blocks(pl.nrec));
+    }
+    CK(ctx->shot_supd.ensure(n_supd * sizeof(float)));
+    CK(cudaMemcpyAsync(ctx->shot_supd.p, hsupd.data(), n_supd * sizeof(float), cudaMemcpyHostToDevice, s));
+    CK(ctx->supd_part.ensure(static_cast<size_t>(nb_big) * 3 * (nt_big + 1) * sizeof(float)));
+    CK(ctx->supd_coef.ensure(static_cast<size_t>(nt_big + 1) * sizeof(float2)));
+    CK(ctx->supd_k.ensure(2 * static_cast<size_t>(nt_big) * sizeof(float)));
   }
   CK(cudaMemcpyAsync(ctx->shot_cpmlx.p, hcpml.data(), n_cpmlx * sizeof(float), cudaMemcpyHostToDevice, s));
   ctx->with_obs = with_obs;
@@ -982,6 +1038,14 @@ int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
     sh.src_x = pl.geom->x_src - pl.x_off;
     sh.src_szz = ctx->shot_src.as<float>(pl.src_off);
     sh.src_sxx = sh.src_szz + pl.nSteps;
+    if (ctx->p.if_src_update) {
+      const SupdLayout L(pl.nSteps);
+      sh.src_szz_r = ctx->shot_supd.as<float>(pl.supd_off + L.szz);
+      sh.src_sxx_r = ctx->shot_supd.as<float>(pl.supd_off + L.sxx);
+    } else {
+      sh.src_szz_r = sh.src_szz;
+      sh.src_sxx_r = sh.src_sxx;
+    }
     sh.nrec = pl.nrec;
     sh.nSteps = pl.nSteps;
     sh.rec_z = ctx->shot_rec.as<int>(pl.rec_off);
@@ -1147,7 +1211,15 @@ int write_scratch(fwigb_ctx* ctx) {
     TRY_RC(write("Residual_Shot" + id + ".bin", h.data(), per));
     TRY_RC(write("Syn_Shot" + id + ".bin", h.data() + per, per));
     TRY_RC(write("CondObs_Shot" + id + ".bin", h.data() + 2 * per, per));
-    TRY_RC(write("src_updated" + id + ".bin", pl.src_amp.data(), nt));
+    if (p.if_src_update) {
+      std::vector<float> upd(nt);
+      CK(cudaMemcpyAsync(upd.data(), ctx->shot_supd.as<float>(pl.supd_off + SupdLayout(nt).upd), nt * sizeof(float),
+                         cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      TRY_RC(write("src_updated" + id + ".bin", upd.data(), nt));
+    } else {
+      TRY_RC(write("src_updated" + id + ".bin", pl.src_amp.data(), nt));
+    }
   }
   return FWIGB_OK;
 }
@@ -1250,27 +1322,64 @@ int run(fwigb_ctx* ctx, int calc_id) {
           float* obs = ctx->shot_data.as<float>(pl.data_off);
           float* syn = ctx->shot_data.as<float>(pl.data_off + per);
           float* res = ctx->shot_data.as<float>(pl.data_off + 2 * per);
-          if (!ctx->p.if_filter) {
+          if (!ctx->p.if_filter && !ctx->p.if_src_update) {
             launch_residual(s, pl.nrec, nt, obs, syn, res, to, tr, pt, ctx->partials.as<double>());
             launch_sum_partials(s, ctx->partials.as<double>(), nb, d_misfit);
             group_launches += 2;
           } else {
-            // Taper, band-pass obs and syn, residual and misfit, band-pass the
-            // residual, adjoint taper (libCUFD.cu:256-310). The filtered
-            // synthetic replaces the gathers, as in the reference.
+            // Taper; band-pass obs and syn; source-wavelet update of syn and
+            // the wavelet; residual and misfit; adjoint update and band-pass
+            // of the residual; adjoint taper (libCUFD.cu:256-310). The
+            // processed synthetic replaces the gathers, as in the reference.
             float* ta = ctx->filt_tmp.as<float>();
             float* tb = ctx->filt_tmp.as<float>(ctx->filt_tmp_floats);
-            const float* h = ctx->shot_filt.as<float>(pl.filt_off);
+            const float* h = ctx->p.if_filter ? ctx->shot_filt.as<float>(pl.filt_off) : nullptr;
             launch_apply_taper(s, pl.nrec, nt, obs, ta, to, pt);
             launch_apply_taper(s, pl.nrec, nt, syn, syn, to, pt);
-            launch_trace_filter(s, pl.nrec, nt, ta, tb, h);
-            launch_trace_filter(s, pl.nrec, nt, syn, ta, h);
-            CK(cudaMemcpyAsync(syn, ta, per * sizeof(float), cudaMemcpyDeviceToDevice, s));
-            launch_residual(s, pl.nrec, nt, tb, syn, res, nullptr, nullptr, 0, ctx->partials.as<double>());
+            group_launches += 2;
+            const float* ob = ta;  // conditioned observed data
+            float* spare = tb;     // free trace block
+            if (h) {
+              launch_trace_filter(s, pl.nrec, nt, ta, tb, h);
+              launch_trace_filter(s, pl.nrec, nt, syn, ta, h);
+              CK(cudaMemcpyAsync(syn, ta, per * sizeof(float), cudaMemcpyDeviceToDevice, s));
+              ob = tb;
+              spare = ta;
+              group_launches += 2;
+            }
+            float* kresp = ctx->supd_k.as<float>();
+            const float* w2 = nullptr;
+            if (ctx->p.if_src_update) {
+              // source_update (utilities.cu:927-1035): coef from the padded,
+              // tapered spectra; syn and the wavelet through the response.
+              const SupdLayout L(nt);
+              float* b = ctx->shot_supd.as<float>(pl.supd_off);
+              w2 = b + L.w2;
+              launch_src_update_coef(s, pl.nrec, nt, ob, syn, w2, reinterpret_cast<const float2*>(b + L.tw),
+                                     ctx->supd_part.as<float>(), ctx->supd_coef.as<float2>(), kresp);
+              launch_apply_taper(s, pl.nrec, nt, syn, spare, w2, 0);
+              launch_trace_filter(s, pl.nrec, nt, spare, syn, kresp);
+              launch_trace_filter(s, 1, nt, b + L.amp, b + L.upd, kresp);
+              launch_src_terms(s, nt, ctx->p.dt, b + L.upd, b + L.szz, b + L.sxx);
+              group_launches += 7;
+            }
+            launch_residual(s, pl.nrec, nt, ob, syn, res, nullptr, nullptr, 0, ctx->partials.as<double>());
             launch_sum_partials(s, ctx->partials.as<double>(), nb, d_misfit);
-            launch_trace_filter(s, pl.nrec, nt, res, ta, h);
-            launch_apply_taper(s, pl.nrec, nt, ta, res, tr, pt);
-            group_launches += 8;
+            group_launches += 2;
+            // The conditioned obs is no longer needed: both blocks are free.
+            if (w2) {  // source_update_adj (utilities.cu:1037-1080), amp_ratio 1
+              launch_apply_taper(s, pl.nrec, nt, res, ta, w2, 0);
+              launch_trace_filter(s, pl.nrec, nt, ta, res, kresp);
+              group_launches += 2;
+            }
+            const float* last = res;
+            if (h) {
+              launch_trace_filter(s, pl.nrec, nt, res, ta, h);
+              last = ta;
+              ++group_launches;
+            }
+            launch_apply_taper(s, pl.nrec, nt, last, res, tr, pt);
+            ++group_launches;
           }
         }
       }
@@ -1320,7 +1429,10 @@ int run(fwigb_ctx* ctx, int calc_id) {
                          reinterpret_cast<uint64_t>(ctx->grads.p), reinterpret_cast<uint64_t>(ctx->scal.p),
                          reinterpret_cast<uint64_t>(ctx->g_slots.p), reinterpret_cast<uint64_t>(ctx->shot_filt.p),
                          reinterpret_cast<uint64_t>(ctx->filt_tmp.p), static_cast<uint64_t>(ctx->filt_tmp_floats),
-                         static_cast<uint64_t>(pl0.filt_off)})
+                         static_cast<uint64_t>(pl0.filt_off), static_cast<uint64_t>(ctx->p.if_src_update),
+                         reinterpret_cast<uint64_t>(ctx->shot_supd.p), reinterpret_cast<uint64_t>(ctx->supd_part.p),
+                         reinterpret_cast<uint64_t>(ctx->supd_coef.p), reinterpret_cast<uint64_t>(ctx->supd_k.p),
+                         static_cast<uint64_t>(pl0.supd_off)})
         key.push_back(v);
       const size_t pack_words = ctx->pack1.size() * sizeof(SweepPack<1>) / sizeof(uint64_t);
       const uint64_t* pw = reinterpret_cast<const uint64_t*>(ctx->pack1.data());
@@ -1509,6 +1621,7 @@ int fwigb_destroy(fwigb_ctx* ctx) {
   for (DevBuf* b : {&ctx->media, &ctx->stage, &ctx->cpml, &ctx->grads, &ctx->scal, &ctx->partials,
                     &ctx->shot_src, &ctx->shot_rec, &ctx->shot_blk, &ctx->shot_data, &ctx->shot_taper,
                     &ctx->shot_gstf, &ctx->shot_cpmlx, &ctx->shot_filt, &ctx->filt_tmp, &ctx->scratch_tmp,
+                    &ctx->shot_supd, &ctx->supd_part, &ctx->supd_coef, &ctx->supd_k,
                     &ctx->g_fields,
                     &ctx->g_store, &ctx->g_grads,
                     &ctx->g_slots})

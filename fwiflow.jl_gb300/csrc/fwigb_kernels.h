@@ -105,6 +105,8 @@ struct ShotD {
   int src_z, src_x;       // source cell (padded-grid indices)
   const float* src_szz;   // per step: 1500^2 * amp * dt (add_source, utilities.cu:528-538)
   const float* src_sxx;   // per step: 3 * 1500^2 * amp * dt
+  const float* src_szz_r; // the terms the reverse reconstruction subtracts: src_szz / src_sxx, or
+  const float* src_sxx_r; // those of the updated wavelet under the source update (libCUFD.cu:326-328, 391-394)
   int nrec, nSteps;
   const int* rec_z;       // receiver cells
   const int* rec_x;
@@ -226,6 +228,14 @@ void launch_apply_taper(cudaStream_t s, int nrec, int nSteps, const float* in, f
 // Band-pass of nrec traces of nt samples: y = x circularly convolved with the
 // impulse response h (2 nt floats); x and y distinct.
 void launch_trace_filter(cudaStream_t s, int nrec, int nt, const float* x, float* y, const float* h);
+// Source-wavelet update of one shot: spectra partial sums into part
+// (src_spectra_blocks(nrec) x 3 x (nt + 1) floats), coef (nt + 1), and the
+// update's impulse response kresp (2 nt floats). w2: the padded-length taper
+// (nt floats); tw: the twiddle table (cos, sin)(2 pi k / 2 nt), 2 nt entries.
+int src_spectra_blocks(int nrec);
+void launch_src_update_coef(cudaStream_t s, int nrec, int nt, const float* obs, const float* syn, const float* w2,
+                            const float2* tw, float* part, float2* coef, float* kresp);
+void launch_src_terms(cudaStream_t s, int nt, float dt, const float* amp, float* szz, float* sxx);
 
 // Column-major float grid (stride ldz) -> row-major double.
 void launch_to_rowmajor(cudaStream_t s, int nz, int nx, int ldz, const float* src, double* dst, double scale);

@@ -372,8 +372,8 @@ __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int 
   float e_own = 0.0f, gmu_own = 0.0f;
   if (interior || src || k >= 0) {
     if (src) {
-      szz -= sh.src_szz[it];
-      sxx -= sh.src_sxx[it];
+      szz -= sh.src_szz_r[it];
+      sxx -= sh.src_sxx_r[it];
     }
     if (interior) {
       const float dvz_dz = sdm(s_vz, b, 1, g.rdz);
@@ -755,8 +755,8 @@ __device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int 
   const float* s_sxx_a = sm + 3 * N;
   const float* s_sxz_a = sm + 4 * N;
   if (special && z == sh.src_z && x == sh.src_x) {
-    szz -= sh.src_szz[it];
-    sxx -= sh.src_sxx[it];
+    szz -= sh.src_szz_r[it];
+    sxx -= sh.src_sxx_r[it];
   }
   const float dvz_dz = sdm(s_vz, b, 1, g.rdz);
   const float dvx_dx = sdm(s_vx, b, kBoxZ, g.rdx);
@@ -1083,6 +1083,171 @@ __global__ void __launch_bounds__(kFilt) k_trace_filter(int nt, const float* __r
   if (t < nt) y[static_cast<size_t>(r) * nt + t] = acc;
 }
 
+// Source-wavelet update (source_update, utilities.cu:927-1035). Traces are
+// zero-padded to M = 2 nt and tapered by w2 (cuda_window over M, ratio 0.01;
+// only its first nt values meet data); the spectra O_r(f), C_r(f) of observed
+// and synthetic traces, f = 0 .. nt, are direct DFTs
+//   X(f) = sum_{t < nt} w2[t] x[t] e^{-2 pi i f t / M},
+// an FP32 GEMM of the twiddle table (cos, sin)(2 pi k / M), k = f t mod M,
+// against the traces. Block: 64 frequencies x 32 traces, samples in chunks of
+// 32 staged in shared memory; thread (fg, rg) = (tid & 15, tid >> 4) holds the
+// four spectra (O, C; re, im) of frequencies f0 + fg + 16 i (i < 4) for traces
+// r0 + rg + 16 j (j < 2). Each block writes its traces' partial sums of
+//   num(f) = sum_r conj(C_r) O_r,  den(f) = sum_r |C_r|^2
+// to part[(blockIdx.y * 3 + {0: Re num, 1: Im num, 2: den}) * (nt + 1) + f].
+constexpr int kSpF = 64, kSpR = 32, kSpT = 32, kSpPad = kSpT + 4;
+__global__ void __launch_bounds__(256) k_src_spectra(int nt, int nrec, const float* __restrict__ obs,
+                                                     const float* __restrict__ syn, const float* __restrict__ w2,
+                                                     const float2* __restrict__ tw, float* __restrict__ part) {
+  __shared__ __align__(16) float sc[kSpF][kSpPad];
+  __shared__ __align__(16) float ss[kSpF][kSpPad];
+  __shared__ __align__(16) float so[kSpR][kSpPad];
+  __shared__ __align__(16) float sd[kSpR][kSpPad];
+  __shared__ float red[3][16][kSpF];
+  const int tid = threadIdx.x, fg = tid & 15, rg = tid >> 4;
+  const int f0 = blockIdx.x * kSpF, r0 = blockIdx.y * kSpR;
+  const int nf = nt + 1;
+  const unsigned M = 2u * static_cast<unsigned>(nt);
+  float acc[4][2][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.0f;
+  for (int t0 = 0; t0 < nt; t0 += kSpT) {
+    for (int e = tid; e < kSpF * kSpT; e += 256) {
+      const int fl = e / kSpT, tl = e % kSpT, f = f0 + fl, t = t0 + tl;
+      float2 v = make_float2(0.0f, 0.0f);
+      if (f < nf && t < nt) v = tw[(static_cast<unsigned>(f) * static_cast<unsigned>(t)) % M];
+      sc[fl][tl] = v.x;
+      ss[fl][tl] = v.y;
+    }
+    for (int e = tid; e < kSpR * kSpT; e += 256) {
+      const int rl = e / kSpT, tl = e % kSpT, r = r0 + rl, t = t0 + tl;
+      float o = 0.0f, d = 0.0f;
+      if (r < nrec && t < nt) {
+        const size_t q = static_cast<size_t>(r) * nt + t;
+        const float w = w2[t];
+        o = obs[q] * w;
+        d = syn[q] * w;
+      }
+      so[rl][tl] = o;
+      sd[rl][tl] = d;
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int tl = 0; tl < kSpT; tl += 4) {
+      float4 c[4], sn[4], o[2], d[2];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        c[i] = *reinterpret_cast<const float4*>(&sc[fg + 16 * i][tl]);
+        sn[i] = *reinterpret_cast<const float4*>(&ss[fg + 16 * i][tl]);
+      }
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        o[j] = *reinterpret_cast<const float4*>(&so[rg + 16 * j][tl]);
+        d[j] = *reinterpret_cast<const float4*>(&sd[rg + 16 * j][tl]);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          float* a = acc[i][j];
+          a[0] = fmaf(o[j].x, c[i].x, a[0]);
+          a[1] = fmaf(-o[j].x, sn[i].x, a[1]);
+          a[2] = fmaf(d[j].x, c[i].x, a[2]);
+          a[3] = fmaf(-d[j].x, sn[i].x, a[3]);
+          a[0] = fmaf(o[j].y, c[i].y, a[0]);
+          a[1] = fmaf(-o[j].y, sn[i].y, a[1]);
+          a[2] = fmaf(d[j].y, c[i].y, a[2]);
+          a[3] = fmaf(-d[j].y, sn[i].y, a[3]);
+          a[0] = fmaf(o[j].z, c[i].z, a[0]);
+          a[1] = fmaf(-o[j].z, sn[i].z, a[1]);
+          a[2] = fmaf(d[j].z, c[i].z, a[2]);
+          a[3] = fmaf(-d[j].z, sn[i].z, a[3]);
+          a[0] = fmaf(o[j].w, c[i].w, a[0]);
+          a[1] = fmaf(-o[j].w, sn[i].w, a[1]);
+          a[2] = fmaf(d[j].w, c[i].w, a[2]);
+          a[3] = fmaf(-d[j].w, sn[i].w, a[3]);
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float nre = 0.0f, nim = 0.0f, den = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const float Or = acc[i][j][0], Oi = acc[i][j][1], Cr = acc[i][j][2], Ci = acc[i][j][3];
+      nre += Cr * Or + Ci * Oi;
+      nim += Cr * Oi - Ci * Or;
+      den += Cr * Cr + Ci * Ci;
+    }
+    red[0][rg][fg + 16 * i] = nre;
+    red[1][rg][fg + 16 * i] = nim;
+    red[2][rg][fg + 16 * i] = den;
+  }
+  __syncthreads();
+  if (tid < 3 * kSpF) {
+    const int q = tid / kSpF, fl = tid % kSpF, f = f0 + fl;
+    float v = 0.0f;
+    for (int u = 0; u < 16; ++u) v += red[q][u][fl];
+    if (f < nf) part[(static_cast<size_t>(blockIdx.y) * 3 + q) * nf + f] = v;
+  }
+}
+
+// coef(f) = num(f) / (den(f) + 1e-6) over the trace blocks' partial sums,
+// added in block order (cuda_spectrum_update, utilities.cu:768-826).
+__global__ void k_src_coef(int nf, int nblk, const float* __restrict__ part, float2* __restrict__ coef) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  float nre = 0.0f, nim = 0.0f, den = 0.0f;
+  for (int b = 0; b < nblk; ++b) {
+    nre += part[(static_cast<size_t>(b) * 3 + 0) * nf + f];
+    nim += part[(static_cast<size_t>(b) * 3 + 1) * nf + f];
+    den += part[(static_cast<size_t>(b) * 3 + 2) * nf + f];
+  }
+  den += 1e-6f;
+  coef[f] = make_float2(nre / den, nim / den);
+}
+
+// Impulse response of the update, the length-M inverse transform of the
+// Hermitian spectrum coef(0 .. nt) divided by M (the C2R + cuda_normalize
+// pair): k[n] = (coef_0 + coef_nt (-1)^n + 2 sum_{f=1}^{nt-1} Re(coef_f
+// e^{2 pi i f n / M})) / M, accumulated in double. Multiplying a padded
+// trace's spectrum by coef and cropping is then y[t] = sum_{m < nt} x[m]
+// k[(t - m) mod M] (k_trace_filter).
+__global__ void k_src_response(int nt, const float2* __restrict__ coef, const float2* __restrict__ tw,
+                               float* __restrict__ kresp) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  const int M = 2 * nt;
+  if (n >= M) return;
+  double acc = static_cast<double>(coef[0].x) + static_cast<double>(coef[nt].x) * ((n & 1) ? -1.0 : 1.0);
+  int k = 0;
+  for (int f = 1; f < nt; ++f) {
+    k += n;
+    if (k >= M) k -= M;
+    const float2 c = coef[f], w = tw[k];
+    acc += 2.0 * (static_cast<double>(c.x) * w.x - static_cast<double>(c.y) * w.y);
+  }
+  kresp[n] = static_cast<float>(acc / M);
+}
+
+// The updated wavelet's source terms for the reverse reconstruction, as the
+// add_source arithmetic forms them (utilities.cu:528-555): 1500^2 amp dt in
+// float, and 3 * 1500^2 * amp * dt in double rounded once.
+__global__ void k_src_terms(int nt, float dt, const float* __restrict__ amp, float* __restrict__ szz,
+                            float* __restrict__ sxx) {
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= nt) return;
+  const float scale = 2250000.0f;
+  const float a = amp[it];
+  szz[it] = __fmul_rn(__fmul_rn(scale, a), dt);
+  sxx[it] = static_cast<float>(__dmul_rn(__dmul_rn(__dmul_rn(3.0, static_cast<double>(scale)), static_cast<double>(a)),
+                                         static_cast<double>(dt)));
+}
+
 // Adds the per-shot gradients and / or illuminations of a shot group into
 // the global ones, in group order (deterministic): shot k's sub-grid column j
 // is global padded column x_off[k] + j.
@@ -1306,6 +1471,20 @@ void launch_residual(cudaStream_t s, int nrec, int nSteps, const float* obs, flo
 void launch_apply_taper(cudaStream_t s, int nrec, int nSteps, const float* in, float* out, const float* taper,
                         int per_trace) {
   k_apply_taper<<<residual_blocks(nrec * nSteps), kResThreads, 0, s>>>(nrec, nSteps, in, out, taper, per_trace);
+}
+
+int src_spectra_blocks(int nrec) { return (nrec + kSpR - 1) / kSpR; }
+
+void launch_src_update_coef(cudaStream_t s, int nrec, int nt, const float* obs, const float* syn, const float* w2,
+                            const float2* tw, float* part, float2* coef, float* kresp) {
+  const int nf = nt + 1, nblk = src_spectra_blocks(nrec);
+  k_src_spectra<<<dim3((nf + kSpF - 1) / kSpF, nblk), 256, 0, s>>>(nt, nrec, obs, syn, w2, tw, part);
+  k_src_coef<<<(nf + 255) / 256, 256, 0, s>>>(nf, nblk, part, coef);
+  k_src_response<<<(2 * nt + 63) / 64, 64, 0, s>>>(nt, coef, tw, kresp);
+}
+
+void launch_src_terms(cudaStream_t s, int nt, float dt, const float* amp, float* szz, float* sxx) {
+  k_src_terms<<<(nt + 255) / 256, 256, 0, s>>>(nt, dt, amp, szz, sxx);
 }
 
 void launch_trace_filter(cudaStream_t s, int nrec, int nt, const float* x, float* y, const float* h) {

@@ -557,6 +557,7 @@ struct oracle_para {
   int if_win;
   int if_filter;     // "filter" key present (Parameter.cpp:155-167)
   float filter[4];   // band-pass corner frequencies f0 < f1 <= f2 < f3 [Hz]
+  int if_src_update; // "if_src_update" (Parameter.cpp:170-174)
 };
 
 struct oracle_shot {
@@ -620,11 +621,104 @@ static void bp_filter(float* data, int nt, int nrec, float dt, const float* fc) 
   }
 }
 
+// Source-wavelet update of one shot (source_update, utilities.cu:927-1035, with
+// cuda_spectrum_update :768-840). The observed and synthetic traces o, d
+// [nrec][nt] (already tapered / filtered) are zero-padded to M = 2 nt and
+// tapered over the padded length (cuda_window, ratio 0.01); their spectra
+// O_r, C_r (float, as cuFFT returns them) give per frequency f = 0 .. nt
+//   coef[f] = sum_r conj(C_r) O_r / (sum_r |C_r|^2 + 1e-6)   (float).
+// The padded, tapered synthetic and the (unpadded-tapered) wavelet become
+// IFFT(spectrum * coef) cropped to nt and divided by M: restated as the
+// circular convolution with k = IFFT(coef) / M, accumulated in double. d and
+// src are replaced; k is returned for the adjoint (src_update_adj).
+static std::vector<double> src_update(float* d, const float* o, float* src, int nt, int nrec, float dt) {
+  const int M = 2 * nt;
+  const double kTwoPi = 6.283185307179586476925286766559;
+  std::vector<double> cs(M), sn(M);
+  for (int k = 0; k < M; ++k) {
+    cs[k] = std::cos(kTwoPi * k / M);
+    sn[k] = std::sin(kTwoPi * k / M);
+  }
+  std::vector<float> op(static_cast<size_t>(nrec) * M, 0.0f), dp(static_cast<size_t>(nrec) * M, 0.0f);
+  for (int r = 0; r < nrec; ++r)
+    for (int t = 0; t < nt; ++t) {
+      op[static_cast<size_t>(r) * M + t] = o[static_cast<size_t>(r) * nt + t];
+      dp[static_cast<size_t>(r) * M + t] = d[static_cast<size_t>(r) * nt + t];
+    }
+  taper(op.data(), M, nrec, dt, 0.01f);
+  taper(dp.data(), M, nrec, dt, 0.01f);
+  std::vector<double> cre(nt + 1), cim(nt + 1);
+  for (int f = 0; f <= nt; ++f) {
+    double nre = 0.0, nim = 0.0, den = 0.0;
+    for (int r = 0; r < nrec; ++r) {
+      double ore = 0.0, oim = 0.0, dre = 0.0, dim = 0.0;
+      const float* orow = op.data() + static_cast<size_t>(r) * M;
+      const float* drow = dp.data() + static_cast<size_t>(r) * M;
+      for (int t = 0; t < nt; ++t) {  // the padded half is zero
+        const int k = static_cast<int>((static_cast<long long>(f) * t) % M);
+        ore += orow[t] * cs[k];
+        oim -= orow[t] * sn[k];
+        dre += drow[t] * cs[k];
+        dim -= drow[t] * sn[k];
+      }
+      const double Or = static_cast<float>(ore), Oi = static_cast<float>(oim);
+      const double Cr = static_cast<float>(dre), Ci = static_cast<float>(dim);
+      nre += Cr * Or + Ci * Oi;
+      nim += Cr * Oi - Ci * Or;
+      den += Cr * Cr + Ci * Ci;
+    }
+    const float denf = static_cast<float>(den) + 1e-6f;
+    cre[f] = static_cast<float>(static_cast<float>(nre) / static_cast<double>(denf));
+    cim[f] = static_cast<float>(static_cast<float>(nim) / static_cast<double>(denf));
+  }
+  // k[n] = (coef_0 + coef_nt (-1)^n + 2 sum_{f=1}^{nt-1} Re(coef_f e^{2 pi i f n / M})) / M
+  std::vector<double> kr(M);
+  for (int n = 0; n < M; ++n) {
+    double acc = cre[0] + cre[nt] * ((n & 1) ? -1.0 : 1.0);
+    for (int f = 1; f < nt; ++f) {
+      const int k = static_cast<int>((static_cast<long long>(f) * n) % M);
+      acc += 2.0 * (cre[f] * cs[k] - cim[f] * sn[k]);
+    }
+    kr[n] = acc / M;
+  }
+  auto conv = [&](const float* x, float* y) {
+    for (int t = 0; t < nt; ++t) {
+      double acc = 0.0;
+      for (int m = 0; m < nt; ++m) acc += static_cast<double>(x[m]) * kr[(t - m + M) % M];
+      y[t] = static_cast<float>(acc);
+    }
+  };
+  for (int r = 0; r < nrec; ++r) conv(dp.data() + static_cast<size_t>(r) * M, d + static_cast<size_t>(r) * nt);
+  std::vector<float> s0(src, src + nt);
+  conv(s0.data(), src);
+  return kr;
+}
+
+// source_update_adj (utilities.cu:1037-1080): residual traces zero-padded to
+// 2 nt, tapered (ratio 0.01), times coef in frequency (not its conjugate), back,
+// cropped and divided by 2 nt (amp_ratio is 1, libCUFD.cu:286): the circular
+// convolution with the k of src_update.
+static void src_update_adj(float* res, int nt, int nrec, float dt, const std::vector<double>& kr) {
+  const int M = 2 * nt;
+  std::vector<float> rp(M);
+  for (int r = 0; r < nrec; ++r) {
+    float* x = res + static_cast<size_t>(r) * nt;
+    std::fill(rp.begin(), rp.end(), 0.0f);
+    std::copy(x, x + nt, rp.begin());
+    taper(rp.data(), M, 1, dt, 0.01f);
+    for (int t = 0; t < nt; ++t) {
+      double acc = 0.0;
+      for (int m = 0; m < nt; ++m) acc += static_cast<double>(rp[m]) * kr[(t - m + M) % M];
+      x[t] = static_cast<float>(acc);
+    }
+  }
+}
+
 static int cufd_impl(const oracle_para* p, const oracle_shot* shots, int group_size, const int* shot_ids,
                      const double* Lambda, const double* Mu, const double* Den, const double* stf, int calc_id,
                      const float* const* obs, float* const* syn_out, float* const* res_out, double* misfit,
                      double* grad_Lambda, double* grad_Mu, double* grad_Den, double* grad_stf, int nthreads,
-                     double* illum) {
+                     double* illum, float* const* src_out) {
   if (calc_id < 0 || calc_id > 2 || !p) return ORACLE_BAD_ARG;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -757,6 +851,13 @@ static int cufd_impl(const oracle_para* p, const oracle_shot* shots, int group_s
       bp_filter(o.data(), nSteps, nrec, g.dt, p->filter);
       bp_filter(data.data(), nSteps, nrec, g.dt, p->filter);
     }
+    // Source-wavelet update (libCUFD.cu:279-286): the synthetic and the
+    // wavelet change; the reverse reconstruction below subtracts the updated
+    // wavelet, as the reference copies it back into the host source it uses
+    // there (libCUFD.cu:326-328, 391-394).
+    std::vector<double> kr;
+    if (p->if_src_update) kr = src_update(data.data(), o.data(), src.data(), nSteps, nrec, g.dt);
+    if (src_out && src_out[is]) std::memcpy(src_out[is], src.data(), nSteps * sizeof(float));
     std::vector<float> res(data.size());
     for (int r = 0; r < nrec; ++r)
       for (int it = 0; it < nSteps; ++it) {
@@ -764,6 +865,7 @@ static int cufd_impl(const oracle_para* p, const oracle_shot* shots, int group_s
         res[k] = (it == 0) ? 0.0f : o[k] - data[k];
       }
     l2 += objective(res.data(), nrec * nSteps);
+    if (p->if_src_update) src_update_adj(res.data(), nSteps, nrec, g.dt, kr);  // libCUFD.cu:296-299
     if (p->if_filter) bp_filter(res.data(), nSteps, nrec, g.dt, p->filter);  // libCUFD.cu:301-304
     if (p->if_win)
       taper_windowed(res.data(), nSteps, nrec, g.dt, 0.1f, sh.win_start, sh.win_end, sh.weights);
@@ -827,7 +929,7 @@ int oracle_cufd(const oracle_para* p, const oracle_shot* shots, int group_size, 
                 const float* const* obs, float* const* syn_out, float* const* res_out, double* misfit,
                 double* grad_Lambda, double* grad_Mu, double* grad_Den, double* grad_stf, int nthreads) {
   return cufd_impl(p, shots, group_size, shot_ids, Lambda, Mu, Den, stf, calc_id, obs, syn_out, res_out, misfit,
-                   grad_Lambda, grad_Mu, grad_Den, grad_stf, nthreads, nullptr);
+                   grad_Lambda, grad_Mu, grad_Den, grad_stf, nthreads, nullptr, nullptr);
 }
 
 // oracle_cufd that also adds the source illumination of every shot, row-major
@@ -838,7 +940,19 @@ int oracle_cufd_illum(const oracle_para* p, const oracle_shot* shots, int group_
                       double* grad_Lambda, double* grad_Mu, double* grad_Den, double* grad_stf, int nthreads,
                       double* illum) {
   return cufd_impl(p, shots, group_size, shot_ids, Lambda, Mu, Den, stf, calc_id, obs, syn_out, res_out, misfit,
-                   grad_Lambda, grad_Mu, grad_Den, grad_stf, nthreads, illum);
+                   grad_Lambda, grad_Mu, grad_Den, grad_stf, nthreads, illum, nullptr);
+}
+
+// oracle_cufd_illum that also returns each shot's source wavelet as the
+// residual path leaves it (the updated wavelet under if_src_update, else the
+// tapered one) in src_out[i] (nSteps floats, optional).
+int oracle_cufd_full(const oracle_para* p, const oracle_shot* shots, int group_size, const int* shot_ids,
+                     const double* Lambda, const double* Mu, const double* Den, const double* stf, int calc_id,
+                     const float* const* obs, float* const* syn_out, float* const* res_out, double* misfit,
+                     double* grad_Lambda, double* grad_Mu, double* grad_Den, double* grad_stf, int nthreads,
+                     double* illum, float* const* src_out) {
+  return cufd_impl(p, shots, group_size, shot_ids, Lambda, Mu, Den, stf, calc_id, obs, syn_out, res_out, misfit,
+                   grad_Lambda, grad_Mu, grad_Den, grad_stf, nthreads, illum, src_out);
 }
 
 }  // extern "C"

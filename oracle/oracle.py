@@ -37,7 +37,7 @@ class _Para(ctypes.Structure):
     _fields_ = [("nz", ctypes.c_int), ("nx", ctypes.c_int), ("nSteps", ctypes.c_int), ("nPml", ctypes.c_int),
                 ("nPad", ctypes.c_int), ("dz", ctypes.c_float), ("dx", ctypes.c_float), ("dt", ctypes.c_float),
                 ("f0", ctypes.c_float), ("if_win", ctypes.c_int), ("if_filter", ctypes.c_int),
-                ("filter", ctypes.c_float * 4)]
+                ("filter", ctypes.c_float * 4), ("if_src_update", ctypes.c_int)]
 
 
 class _Shot(ctypes.Structure):
@@ -58,6 +58,7 @@ def _load_oracle(precision: str = "reference"):
             raise RuntimeError(f"oracle library not built: {path} (run make -C oracle)")
         lib = ctypes.CDLL(path)
         lib.oracle_cufd.restype = ctypes.c_int
+        lib.oracle_cufd_full.restype = ctypes.c_int
         _oracles[precision] = lib
     return _oracles[precision]
 
@@ -135,7 +136,8 @@ def _run_group(p: dict, shots: list, ids: Sequence[int], nz: int, nx: int, nt: i
     """One oracle_cufd call over shots sharing one grid and record length."""
     fl = p.get("filter")
     para = _Para(nz, nx, nt, p["nPml"], p["nPad"], p["dz"], p["dx"], p["dt"], p["f0"], int(p["if_win"]),
-                 int(fl is not None), (ctypes.c_float * 4)(*(fl if fl is not None else [0.0] * 4)))
+                 int(fl is not None), (ctypes.c_float * 4)(*(fl if fl is not None else [0.0] * 4)),
+                 int(p.get("if_src_update", False)))
     keep = []
     carr = (_Shot * len(shots))()
     for i, s in enumerate(shots):
@@ -160,6 +162,14 @@ def _run_group(p: dict, shots: list, ids: Sequence[int], nz: int, nx: int, nt: i
     syn_ptrs = (ctypes.POINTER(ctypes.c_float) * max(n, 1))()
     for i, a in enumerate(syn):
         syn_ptrs[i] = _fptr(a)
+    res = [np.zeros(s["nrec"] * nt, dtype=np.float32) for s in shots]
+    res_ptrs = (ctypes.POINTER(ctypes.c_float) * max(n, 1))()
+    for i, a in enumerate(res):
+        res_ptrs[i] = _fptr(a)
+    src = [np.zeros(nt, dtype=np.float32) for _ in shots]
+    src_ptrs = (ctypes.POINTER(ctypes.c_float) * max(n, 1))()
+    for i, a in enumerate(src):
+        src_ptrs[i] = _fptr(a)
     misfit = ctypes.c_double(0.0)
     g_lam = np.zeros((nz, nx))
     g_mu = np.zeros((nz, nx))
@@ -168,12 +178,13 @@ def _run_group(p: dict, shots: list, ids: Sequence[int], nz: int, nx: int, nt: i
     cids = np.asarray(ids, dtype=np.int32)
     lib = _load_oracle(precision)
     args = (ctypes.byref(para), carr, n, _iptr(cids), _dptr(lam), _dptr(mu), _dptr(den), _dptr(stf), int(calc_id),
-            obs_ptrs, syn_ptrs, None, ctypes.byref(misfit), _dptr(g_lam), _dptr(g_mu), _dptr(g_den), _dptr(g_stf),
+            obs_ptrs, syn_ptrs, res_ptrs, ctypes.byref(misfit), _dptr(g_lam), _dptr(g_mu), _dptr(g_den), _dptr(g_stf),
             int(nthreads))
-    rc = lib.oracle_cufd(*args) if illum is None else lib.oracle_cufd_illum(*args, _dptr(illum))
+    rc = lib.oracle_cufd_full(*args, None if illum is None else _dptr(illum), src_ptrs)
     if rc != 0:
         raise RuntimeError(f"oracle_cufd failed with status {rc}")
-    return misfit.value, g_lam, g_mu, g_den, g_stf, [a.reshape(s["nrec"], nt) for a, s in zip(syn, shots)]
+    return (misfit.value, g_lam, g_mu, g_den, g_stf, [a.reshape(s["nrec"], nt) for a, s in zip(syn, shots)],
+            (src, [a.reshape(s["nrec"], nt) for a, s in zip(res, shots)]))
 
 
 def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads: int = 0,
@@ -186,7 +197,10 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
     are read from `data_dir_name/Shot<id>.bin` unless `obs` is given; for
     calc_id 2 the gathers are written there when `write_files`.
     Returns misfit, g_lambda, g_mu, g_den, g_stf and (optionally) gathers
-    (shot k's gather is [nrec][its record length]).
+    (shot k's gather is [nrec][its record length]; for calc_id 0/1 the
+    processed synthetic, with "wavelets": each shot's source wavelet as the
+    residual path leaves it, updated under if_src_update, and "residuals":
+    the adjoint sources).
     precision "fp32" runs the FP32-only build (no double promotions).
     want_illum adds "illum": the source illumination (sum over shots and
     forward steps of vz^2 + vx^2 after each velocity update), [nz][nx].
@@ -207,14 +221,15 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
     extended = any("nSteps" in s or "win_x0" in s for s in shots)
     illum = np.zeros((nz, nx)) if want_illum else None
     if not extended:
-        misfit, g_lam, g_mu, g_den, g_stf, gathers = _run_group(p, shots, shot_ids, nz, nx, nt, lam, mu, den, stf,
-                                                                calc_id, obs, nthreads, precision, illum)
+        misfit, g_lam, g_mu, g_den, g_stf, gathers, (wavelets, residuals) = _run_group(p, shots, shot_ids, nz, nx, nt, lam, mu,
+                                                                          den, stf, calc_id, obs, nthreads,
+                                                                          precision, illum)
     else:
         # Each shot alone on its sub-model, for its own record length.
         misfit = 0.0
         g_lam, g_mu, g_den = np.zeros((nz, nx)), np.zeros((nz, nx)), np.zeros((nz, nx))
         g_stf = np.zeros_like(stf)
-        gathers = []
+        gathers, wavelets, residuals = [], [], []
         nPml = p["nPml"]
         for k, (sid, s) in enumerate(zip(shot_ids, shots)):
             ntk = s.get("nSteps", nt)
@@ -228,7 +243,7 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
             stf_k = np.ascontiguousarray(stf[sid:sid + 1, :ntk])
             ob = None if obs is None else [obs[k]]
             il = None if illum is None else np.zeros((nz, nxk))
-            m, gl, gm, gd, gs, gth = _run_group(p, [sub], [0], nz, nxk, ntk, np.ascontiguousarray(lam[:, cols]),
+            m, gl, gm, gd, gs, gth, (wv, rs) = _run_group(p, [sub], [0], nz, nxk, ntk, np.ascontiguousarray(lam[:, cols]),
                                                np.ascontiguousarray(mu[:, cols]), np.ascontiguousarray(den[:, cols]),
                                                stf_k, calc_id, ob, nthreads, precision, il)
             if il is not None:
@@ -239,6 +254,8 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
             g_den[:, cols] += gd
             g_stf[sid, :ntk] += gs[0]
             gathers += gth
+            wavelets += wv
+            residuals += rs
     out = {"misfit": misfit, "g_lambda": g_lam, "g_mu": g_mu, "g_den": g_den, "g_stf": g_stf}
     if illum is not None:
         out["illum"] = illum
@@ -247,6 +264,9 @@ def cufd(calc_id: int, lam, mu, den, stf, shot_ids, para_fname: str, *, nthreads
             a.astype(np.float32).tofile(os.path.join(p["data_dir_name"], f"Shot{sid}.bin"))
     if want_gathers:
         out["gathers"] = gathers
+        if calc_id in (0, 1):
+            out["wavelets"] = wavelets
+            out["residuals"] = residuals
     return out
 
 

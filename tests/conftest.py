@@ -64,12 +64,14 @@ def golden_workload(name, tmp_path):
             s["win_end"] = list(rng.uniform(0.6 * T, 1.1 * T, n))
             s["weights"] = list(rng.uniform(0.5, 1.5, n))
     para = w.write_files(str(tmp_path))
-    if "window_seed" in meta or "filter" in meta:
+    if "window_seed" in meta or "filter" in meta or meta.get("src_update"):
         p = json.load(open(para))
         if "window_seed" in meta:
             p["if_win"] = True
         if "filter" in meta:
             p["filter"] = meta["filter"]
+        if meta.get("src_update"):
+            p["if_src_update"] = True
         with open(para, "w") as f:
             f.write(json.dumps(p, separators=(",", ":")))
     if meta["builder"] == "tiny":

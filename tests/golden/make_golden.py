@@ -17,6 +17,10 @@ Cases (all seeded, see fwiflow.jl_gb300/synthetic.py):
                  utilities.cu:872-923, applied at libCUFD.cu:273-277 and 301-304)
   tiny_scratch   the tiny_filter case with a "scratch_dir_name": the scratch outputs of its
                  gradient call (libCUFD.cu:493-511) per shot
+  tiny_srcupd    2 shots with "if_src_update": the per-frequency source-wavelet update of the
+                 residual path (source_update / source_update_adj, utilities.cu:927-1080, applied
+                 at libCUFD.cu:279-299); with its scratch outputs (updated wavelet included)
+  tiny_srcupd_filter  the same with the band-pass filter on as well
   small_layered  the 100x200, 1000-step, 2-shot workload: misfit, norms and a strided
                  subsample of gathers and gradients
 """
@@ -73,9 +77,10 @@ def run_case(w, with_window=False, para_extra=None):
     return para, r2, r0, r1
 
 
-def save_full(name, w, r2, r0, r1, **meta):
+def save_full(name, w, r2, r0, r1, extra=None, **meta):
     np.savez_compressed(
         os.path.join(OUT, f"{name}.npz"),
+        **(extra or {}),
         gathers=np.stack(r2["gathers"]).astype(np.float32),
         misfit=np.float64(r0["misfit"]),
         g_lambda=r1["g_lambda"].astype(np.float32),
@@ -93,6 +98,7 @@ def main():
     if not orc.refhost_available():
         raise SystemExit("oracle/_ref/librefhost_fwi.so missing: build it with oracle/Makefile.refhost")
     cases = set(sys.argv[1:]) or {"tiny_elastic", "tiny_acoustic", "tiny_window", "tiny_filter", "tiny_scratch",
+                                  "tiny_srcupd", "tiny_srcupd_filter",
                                   "small_layered"}
     if "tiny_scratch" in cases:
         kw = dict(nz=32, nx=48, nPml=10, nSteps=200, n_shots=2, seed=3)
@@ -105,6 +111,22 @@ def main():
                 out[f"{name}{sid}"] = np.fromfile(os.path.join(scratch, f"{name}{sid}.bin"), dtype=np.float32)
         np.savez_compressed(os.path.join(OUT, "tiny_scratch.npz"), **out,
                             meta=json.dumps({"builder": "tiny", "filter": FILTER, "kwargs": kw}))
+    for name in ("tiny_srcupd", "tiny_srcupd_filter"):
+        if name not in cases:
+            continue
+        kw = dict(nz=32, nx=48, nPml=10, nSteps=200, n_shots=2, seed=4)
+        w = synthetic.tiny(**kw)
+        scratch = tempfile.mkdtemp()
+        extra_para = {"if_src_update": True, "scratch_dir_name": scratch}
+        meta = {"builder": "tiny", "src_update": True, "kwargs": kw}
+        if name.endswith("_filter"):
+            extra_para["filter"] = meta["filter"] = FILTER
+        _, r2, r0, r1 = run_case(w, para_extra=extra_para)
+        extra = {}
+        for sid in range(len(w.shots)):
+            for f in ("Residual_Shot", "Syn_Shot", "CondObs_Shot", "src_updated"):
+                extra[f"{f}{sid}"] = np.fromfile(os.path.join(scratch, f"{f}{sid}.bin"), dtype=np.float32)
+        save_full(name, w, r2, r0, r1, extra=extra, **meta)
     if "tiny_filter" in cases:
         kw = dict(nz=32, nx=48, nPml=10, nSteps=200, n_shots=2, seed=3)
         w = synthetic.tiny(**kw)

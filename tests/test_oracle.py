@@ -13,13 +13,21 @@ import pytest
 
 from conftest import golden_workload, rel
 
-TINY = ["tiny_elastic", "tiny_acoustic", "tiny_window", "tiny_filter"]
+TINY = ["tiny_elastic", "tiny_acoustic", "tiny_window", "tiny_filter", "tiny_srcupd", "tiny_srcupd_filter"]
 # Oracle vs reference: both are float programs with the same operation order
 # except the mu / rho scatter (atomicAdd in the reference, a gather here).
 TOL_EXACT = 1e-6
 # The band-pass filter: the reference transforms with (emulated) cuFFT, the
 # oracle convolves with the same filter's impulse response in double.
-TOL = {"tiny_filter": 1e-5}
+TOL = {"tiny_filter": 1e-5, "tiny_srcupd_filter": 1e-5}
+# The source-wavelet update also replaces the synthetic by its spectrum times
+# a data-derived coefficient (float products in the reference, a double
+# convolution here); the residual obs - syn then loses digits to cancellation
+# (the synthetic is ~40x the residual in this case), and the wavelet gradient
+# of tiny_srcupd is a small difference of adjoint values: the oracle's own
+# FP32 build sits 1.3e-4 from the oracle there.
+TOL.update({"tiny_srcupd": 3e-5})
+TOL_KEY = {("tiny_srcupd", "g_stf"): 1e-3, ("tiny_srcupd_filter", "g_stf"): 2e-4}
 
 
 @pytest.mark.parametrize("name", TINY)
@@ -35,7 +43,23 @@ def test_oracle_matches_golden(name, orc, tmp_path, fw):
     assert abs(r0["misfit"] - float(d["misfit"])) <= tol * abs(float(d["misfit"]))
     r1 = orc.cufd(1, lam, mu, rho, w.stf, ids, para)
     for k in ("g_lambda", "g_mu", "g_den", "g_stf"):
-        assert rel(r1[k], d[k]) < tol, k
+        assert rel(r1[k], d[k]) < TOL_KEY.get((name, k), tol), k
+
+
+@pytest.mark.parametrize("name", ["tiny_srcupd", "tiny_srcupd_filter"])
+def test_oracle_source_update_matches_reference_scratch(name, orc, tmp_path, fw):
+    """The updated synthetic, the updated wavelet and the adjoint source of
+    the source-wavelet update (utilities.cu:927-1080) against the scratch files
+    the reference wrote for the same gradient call."""
+    d, w, para, moduli = golden_workload(name, tmp_path)
+    ids = list(range(len(w.shots)))
+    lo, mo, ro = moduli(w.vp_obs)
+    orc.cufd(2, lo, mo, ro, w.stf, ids, para, write_files=True)
+    r1 = orc.cufd(1, *moduli(w.vp), w.stf, ids, para, want_gathers=True)
+    for i in ids:
+        assert rel(r1["gathers"][i].ravel(), d[f"Syn_Shot{i}"]) < 1e-6
+        assert rel(r1["wavelets"][i], d[f"src_updated{i}"]) < 1e-6
+        assert rel(r1["residuals"][i].ravel(), d[f"Residual_Shot{i}"]) < 1e-5
 
 
 def test_oracle_matches_golden_small_layered(orc, tmp_path, fw):
