@@ -477,7 +477,7 @@ struct fwigb_ctx {
   int last_calc = -1;
   long long launches = 0;
   int tx[4] = {8, 8, 8, 8};    // tile width per sweep (F1, F2, B, C)
-  int rows[4] = {2, 2, 1, 1};  // depths per thread per sweep (forward: 1 or 2)
+  int rows[4] = {2, 2, 1, 1};  // depths per thread per sweep (1 or 2)
   bool tuned_fwd = false, tuned_bwd = false;
   bool autotune = true;
   // per-kernel event timing
@@ -988,14 +988,14 @@ int plan_groups(fwigb_ctx* ctx, bool adj, std::vector<std::vector<int>>& groups)
 // backward iteration (B, C). Returns the number of launches.
 int launch_sweep(fwigb_ctx* ctx, int w, int tx, int rows, int a, int arg, bool save, unsigned* d_err) {
   cudaStream_t s = ctx->stream;
-  const int variant = (w < 2 && rows == 2) ? w + 4 : w;
+  const int variant = rows == 2 ? w + 4 : w;
   const size_t base = static_cast<size_t>(variant * 3 + tx_slot(tx));
   auto go = [&](const auto& pk, int n, const SweepGrid& gr) {
     switch (w) {
       case 0: return launch_fwd_stress(s, tx, rows, pk, n, gr, arg, save, d_err);
       case 1: return launch_fwd_velocity(s, tx, rows, pk, n, gr, d_err);
-      case 2: return launch_bwd_B(s, tx, pk, n, gr, arg, d_err);
-      default: return launch_bwd_C(s, tx, pk, n, gr, arg, d_err);
+      case 2: return launch_bwd_B(s, tx, rows, pk, n, gr, arg, d_err);
+      default: return launch_bwd_C(s, tx, rows, pk, n, gr, arg, d_err);
     }
   };
   if (a <= 0) return 0;
@@ -1073,7 +1073,7 @@ int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
         ctx->err = why;
         return FWIGB_ERR_CUDA;
       }
-      const TileMaps* per_sweep[kSweepVariants] = {&sm.f1, &sm.f2, &sm.b, &sm.c, &sm.f1w, &sm.f2w};
+      const TileMaps* per_sweep[kSweepVariants] = {&sm.f1, &sm.f2, &sm.b, &sm.c, &sm.f1w, &sm.f2w, &sm.bw, &sm.cw};
       for (int w = 0; w < kSweepVariants; ++w)
         maps[static_cast<size_t>(w * 3 + t) * ctx->group_cap + k] = *per_sweep[w];
     }
@@ -1124,7 +1124,7 @@ int autotune(fwigb_ctx* ctx, int nshots, int nx_max, bool adj) {
   for (cudaEvent_t& e : ev) CK(cudaEventCreate(&e));
   const int kinds_end = (adj && ctx->nSteps_max >= 2) ? 4 : 2;
   for (int kind = ctx->tuned_fwd ? 2 : 0; kind < kinds_end; ++kind) {
-    const int ncand = kind < 2 ? 6 : 3;  // (width, rows) candidates
+    const int ncand = 6;  // (width, rows) candidates
     auto cand = [&](int q, int& tx, int& rows) {
       tx = kTileXs[q % 3];
       rows = q < 3 ? 1 : 2;
@@ -1394,11 +1394,11 @@ int run(fwigb_ctx* ctx, int calc_id) {
         // then res_injection(nSteps-1) + el_stress_adj, source_grad(nSteps-2),
         // reverse velocity of step nSteps-2 ... (libCUFD.cu:353-445), with
         // backward iteration j meaning step nSteps_k - 2 - j of member k.
-        TIMED(3, group_launches += launch_sweep(ctx, 3, ctx->tx[3], 1, G, -1, false, d_err));
+        TIMED(3, group_launches += launch_sweep(ctx, 3, ctx->tx[3], ctx->rows[3], G, -1, false, d_err));
         for (int j = 0; j <= ntop - 2; ++j) {
           const int a = active(j);
-          TIMED(2, group_launches += launch_sweep(ctx, 2, ctx->tx[2], 1, a, j, false, d_err));
-          TIMED(3, group_launches += launch_sweep(ctx, 3, ctx->tx[3], 1, a, j, false, d_err));
+          TIMED(2, group_launches += launch_sweep(ctx, 2, ctx->tx[2], ctx->rows[2], a, j, false, d_err));
+          TIMED(3, group_launches += launch_sweep(ctx, 3, ctx->tx[3], ctx->rows[3], a, j, false, d_err));
         }
       }
       if (adj || ctx->illum) {
@@ -1717,7 +1717,7 @@ int fwigb_sweep_time(fwigb_ctx* ctx, int kind, int reps, double* us_per_launch) 
   }
   cudaStream_t s = ctx->stream;
   unsigned* d_err = reinterpret_cast<unsigned*>(ctx->scal.as<char>() + 16);
-  const int rows = kind < 2 ? ctx->rows[kind] : 1;
+  const int rows = ctx->rows[kind];
   CK(cudaStreamSynchronize(s));
   CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   for (int r = 0; r < reps; ++r) launch_sweep(ctx, kind, ctx->tx[kind], rows, ctx->group_size, 0, false, d_err);
@@ -1759,6 +1759,19 @@ int fwigb_set_graphs(fwigb_ctx* ctx, int enable) {
 int fwigb_tile_rows(const fwigb_ctx* ctx, int* rows) {
   if (!ctx || !rows) return FWIGB_ERR_ARG;
   for (int k = 0; k < 4; ++k) rows[k] = ctx->rows[k];
+  return FWIGB_OK;
+}
+
+int fwigb_set_tile_rows(fwigb_ctx* ctx, const int* rows) {
+  if (!ctx || !rows) return FWIGB_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  for (int k = 0; k < 4; ++k)
+    if (rows[k] != 1 && rows[k] != 2) {
+      ctx->err = "depths per thread must be 1 or 2";
+      return FWIGB_ERR_ARG;
+    }
+  for (int k = 0; k < 4; ++k) ctx->rows[k] = rows[k];
+  ctx->autotune = false;
   return FWIGB_OK;
 }
 

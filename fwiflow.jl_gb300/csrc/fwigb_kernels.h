@@ -150,11 +150,11 @@ struct ShotSlot {
 // sxx, sxz; B vz, vx, szz_a, sxx_a, sxz_a; C vz_a, vx_a, szz, sxx, sxz.
 struct SweepMaps {
   TileMaps f1, f2, b, c;
-  TileMaps f1w, f2w;  // forward sweeps with two-row tiles (kBoxZFwd boxes)
+  TileMaps f1w, f2w, bw, cw;  // the sweeps with two-row tiles (kBoxZFwd boxes)
 };
 // Launch variants of the sweeps: 0 F1, 1 F2, 2 B, 3 C (one row per thread),
-// 4 F1, 5 F2 (two rows per thread).
-constexpr int kSweepVariants = 6;
+// 4 F1, 5 F2, 6 B, 7 C (two rows per thread).
+constexpr int kSweepVariants = 8;
 
 // What one sweep launch reads for up to K shots, passed by value as a
 // __grid_constant__ kernel parameter: the block of shot k reads its slot and
@@ -194,10 +194,10 @@ template <int K>
 int launch_fwd_velocity(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
                         unsigned* err);
 template <int K>
-int launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
+int launch_bwd_B(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err);
 template <int K>
-int launch_bwd_C(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
+int launch_bwd_C(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err);
 // Adds the per-shot gradients (when g_lam is not null) and illuminations (when
 // g_illum is not null) of the first nshots slots into the global ones.

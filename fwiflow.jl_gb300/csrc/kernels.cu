@@ -214,11 +214,13 @@ __device__ __forceinline__ float dd(float p, float q, float s, float t, float r)
 }
 
 // Register budgets (measured on GB300 over the tile widths): forward sweeps
-// 32 registers with one cell per thread (64 warps per SM) and 40 with two,
-// backward sweeps 48 (40 warps per SM; more resident warps beat the loads the
-// compiler could otherwise hoist).
+// 32 registers with one cell per thread (64 warps per SM) and 40 with two;
+// backward sweeps 40 with one cell (48 warps per SM: 8 % faster than 48
+// registers on a 16-shot group, whose sweeps wait on memory latency) and 64
+// with two (32 warps per SM).
 #define FWD_BOUNDS __launch_bounds__(32 * TX, (R == 1 ? 2048 : 1536) / (32 * TX))
-#define BWD_BOUNDS __launch_bounds__(32 * TX, (1280 / (32 * TX)) > 0 ? (1280 / (32 * TX)) : 1)
+#define BWD_BOUNDS \
+  __launch_bounds__(32 * TX, ((R == 1 ? 1536 : 1024) / (32 * TX)) > 0 ? ((R == 1 ? 1536 : 1024) / (32 * TX)) : 1)
 
 // ---------------------------------------------------------------------------
 // F1: el_stress (el_stress.cu:50-88) + add_source (utilities.cu:521-541) +
@@ -347,25 +349,27 @@ __device__ __forceinline__ void fwd_velocity_edge(const SweepPack<K>& P, int sho
 // ---------------------------------------------------------------------------
 // B: add_source(-) + el_stress(isFor=false) with the lambda / mu kernels +
 // to_bnd(stress) + el_velocity_adj. Staged: vz, vx, szz_a, sxx_a, sxz_a.
-template <int TX, int K>
+template <int TX, int K, int R>
 __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
+  constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
-  SWEEP_STAGE(5, kBoxZ, 1)
+  SWEEP_STAGE(5, BOXZ, R)
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
   const Grads& gr = S.gr;
   const int it = S.nSteps - 2 - j;  // this shot's time step at backward iteration j
   const float dt = g.dt;
-  float szz = f.szz[i], sxx = f.sxx[i], sxz = f.sxz[i];
-  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
-  const float gl = gr.lam[i], gm = gr.mu[i], w = m.muw[i], h = m.hs[i];
-  const float va_z = f.vz_a[i], va_x = f.vx_a[i], bA = m.bycA[i], bB = m.bycB[i];
   if (!stage_wait(&bar, err)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
   const float* s_szz_a = sm + 2 * N;
   const float* s_sxx_a = sm + 3 * N;
   const float* s_sxz_a = sm + 4 * N;
+  auto cell = [&](const int z, const size_t i, const int b) {
+  float szz = f.szz[i], sxx = f.sxx[i], sxz = f.sxz[i];
+  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
+  const float gl = gr.lam[i], gm = gr.mu[i], w = m.muw[i], h = m.hs[i];
+  const float va_z = f.vz_a[i], va_x = f.vx_a[i], bA = m.bycA[i], bB = m.bycB[i];
   const bool interior = in_box(z, x, g.zi0, g.zi1, g.xi0, g.xi1);
   const bool src = (z == sh.src_z && x == sh.src_x);
   const int k = ring_index(g, z, x);
@@ -377,9 +381,9 @@ __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int 
     }
     if (interior) {
       const float dvz_dz = sdm(s_vz, b, 1, g.rdz);
-      const float dvx_dx = sdm(s_vx, b, kBoxZ, g.rdx);
+      const float dvx_dx = sdm(s_vx, b, BOXZ, g.rdx);
       const float dvx_dz = sdp(s_vx, b, 1, g.rdz);
-      const float dvz_dx = sdp(s_vz, b, kBoxZ, g.rdx);
+      const float dvz_dx = sdp(s_vz, b, BOXZ, g.rdx);
       szz -= (l2m * dvz_dz + lam * dvx_dx) * dt;
       sxx -= (lam * dvz_dz + l2m * dvx_dx) * dt;
       e_own = dvx_dz + dvz_dx;
@@ -410,18 +414,18 @@ __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int 
         const float hj = hs[i - 1];
         const int bj = b - 1;
         if (hj != 0.0f)
-          acc += w * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, kBoxZ, g.rdx)) * dt * hj);
+          acc += w * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, BOXZ, g.rdx)) * dt * hj);
       }
     }
     if (x - 1 >= g.xi0) {
       const float hj = hs[i - ldz];
-      const int bj = b - kBoxZ;
-      if (hj != 0.0f) acc += w * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, kBoxZ, g.rdx)) * dt * hj);
+      const int bj = b - BOXZ;
+      if (hj != 0.0f) acc += w * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, BOXZ, g.rdx)) * dt * hj);
       if (z - 1 >= g.zi0 && x <= g.xi1) {
         const float h2 = hs[i - ldz - 1];
-        const int b2 = b - kBoxZ - 1;
+        const int b2 = b - BOXZ - 1;
         if (h2 != 0.0f)
-          acc += w * (-s_sxz_a[b2] * (sdp(s_vx, b2, 1, g.rdz) + sdp(s_vz, b2, kBoxZ, g.rdx)) * dt * h2);
+          acc += w * (-s_sxz_a[b2] * (sdp(s_vx, b2, 1, g.rdz) + sdp(s_vz, b2, BOXZ, g.rdx)) * dt * h2);
       }
     }
     gr.mu[i] = acc;
@@ -433,8 +437,8 @@ __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int 
   const bool xp = (x < g.nPml) || (x > g.xpml_hi_s);
   {
     const float Kx = c.K_x[x], Kzh = c.K_zh[z];
-    const float dszz_dx = -sdp(s_szz_a, b, kBoxZ, g.rdx);
-    const float dsxx_dx = -sdp(s_sxx_a, b, kBoxZ, g.rdx);
+    const float dszz_dx = -sdp(s_szz_a, b, BOXZ, g.rdx);
+    const float dsxx_dx = -sdp(s_sxx_a, b, BOXZ, g.rdx);
     const float dsxz_dz = -sdm(s_sxz_a, b, 1, g.rdz);
     float t = lam * dszz_dx / Kx * dt + l2m * dsxx_dx / Kx * dt + amu / Kzh * dsxz_dz * dt;
     const float ax = c.a_x[x], azh = c.a_zh[z];
@@ -449,7 +453,7 @@ __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int 
     const float Kz = c.K_z[z], Kxh = c.K_xh[x];
     const float dszz_dz = -sdp(s_szz_a, b, 1, g.rdz);
     const float dsxx_dz = -sdp(s_sxx_a, b, 1, g.rdz);
-    const float dsxz_dx = -sdm(s_sxz_a, b, kBoxZ, g.rdx);
+    const float dsxz_dx = -sdm(s_sxz_a, b, BOXZ, g.rdx);
     float t = l2m * dszz_dz / Kz * dt + lam * dsxx_dz / Kz * dt + amu / Kxh * dsxz_dx * dt;
     const float az = c.a_z[z], axh = c.a_xh[x];
     if (az != 0.0f) t += az * (-gdp(f.m_dvz_dz, i, 1, g.rdz));
@@ -459,16 +463,21 @@ __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int 
     if (xp) f.m_dsxz_dx[i] = c.b_x[x] * f.m_dsxz_dx[i] + bA * v * dt;
     if (zp) f.m_dszz_dz[i] = c.b_zh[z] * f.m_dszz_dz[i] + bA * v * dt;
   }
+  };
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (z + r < g.nz) cell(z + r, i + r, b + r);
 }
 
 // C: res_injection (utilities.cu:569-580) + el_stress_adj (el_stress_adj.cu:53-97)
 //    + source_grad (utilities.cu:582-593) + el_velocity(isFor=false) with the
 //    density kernel (el_velocity.cu:220-244) + to_bnd(velocity).
 //    Staged: vz_a, vx_a, szz, sxx, sxz.
-template <int TX, int K>
+template <int TX, int K, int R>
 __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
+  constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
-  SWEEP_STAGE(5, kBoxZ, 1)
+  SWEEP_STAGE(5, BOXZ, R)
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
   const Grads& gr = S.gr;
@@ -478,6 +487,13 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
   const int it = S.nSteps - 2 - j;
   const int rev = it >= 1;
   const float dt = g.dt;
+  if (!stage_wait(&bar, err)) return;
+  const float* s_vz_a = sm;
+  const float* s_vx_a = sm + N;
+  const float* s_szz = sm + 2 * N;
+  const float* s_sxx = sm + 3 * N;
+  const float* s_sxz = sm + 4 * N;
+  auto cell = [&](const int z, const size_t i, const int b) {
   float sa = f.szz_a[i], xa = f.sxx_a[i], za = f.sxz_a[i];
   const float bA = m.bycA[i], bB = m.bycB[i], amu = m.aveMu[i], lam = m.lam[i], l2m = m.l2m[i];
   float vz = 0.0f, vx = 0.0f, gd = 0.0f;
@@ -486,12 +502,6 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
     vx = f.vx[i];
     gd = gr.den[i];
   }
-  if (!stage_wait(&bar, err)) return;
-  const float* s_vz_a = sm;
-  const float* s_vx_a = sm + N;
-  const float* s_szz = sm + 2 * N;
-  const float* s_sxx = sm + 3 * N;
-  const float* s_sxz = sm + 4 * N;
   const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
   bool injected = false;
   const int2 rr = bin_range(sh, z, x);
@@ -506,7 +516,7 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
   }
   if (dom) {
     {
-      const float dvz_dx = -sdp(s_vz_a, b, kBoxZ, g.rdx);
+      const float dvz_dx = -sdp(s_vz_a, b, BOXZ, g.rdx);
       const float dvx_dz = -sdp(s_vx_a, b, 1, g.rdz);
       float t = dvz_dx / c.K_x[x] * bA * dt + dvx_dz / c.K_z[z] * bB * dt;
       const float ax = c.a_x[x], az = c.a_z[z];
@@ -520,7 +530,7 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
     if (xb) f.m_dvz_dx[i] = c.b_xh[x] * f.m_dvz_dx[i] + za * amu * dt;
     if (zb) f.m_dvx_dz[i] = c.b_zh[z] * f.m_dvx_dz[i] + za * amu * dt;
     {
-      const float dvx_dx = -sdm(s_vx_a, b, kBoxZ, g.rdx);
+      const float dvx_dx = -sdm(s_vx_a, b, BOXZ, g.rdx);
       const float dvz_dz = -sdm(s_vz_a, b, 1, g.rdz);
       float tx = bB * dvx_dx / c.K_xh[x] * dt;
       float tz = bA * dvz_dz / c.K_zh[z] * dt;
@@ -543,8 +553,8 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
   float tA = 0.0f, tB = 0.0f;
   const int k = ring_index(g, z, x);
   if (interior) {
-    const float ea = sdp(s_szz, b, 1, g.rdz) + sdm(s_sxz, b, kBoxZ, g.rdx);  // dszz_dz + dsxz_dx
-    const float eb = sdm(s_sxz, b, 1, g.rdz) + sdp(s_sxx, b, kBoxZ, g.rdx);  // dsxz_dz + dsxx_dx
+    const float ea = sdp(s_szz, b, 1, g.rdz) + sdm(s_sxz, b, BOXZ, g.rdx);  // dszz_dz + dsxz_dx
+    const float eb = sdm(s_sxz, b, 1, g.rdz) + sdp(s_sxx, b, BOXZ, g.rdx);  // dsxz_dz + dsxx_dx
     vz -= ea * bA * dt;
     vx -= eb * bB * dt;
     tA = -s_vz_a[b] * ea * dt * (-bA * bA * 0.5f);
@@ -569,18 +579,22 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
       if (z - 1 >= g.zi0) {
         const int bj = b - 1;
         const float bAj = m.bycA[i - 1];
-        const float ea = sdp(s_szz, bj, 1, g.rdz) + sdm(s_sxz, bj, kBoxZ, g.rdx);
+        const float ea = sdp(s_szz, bj, 1, g.rdz) + sdm(s_sxz, bj, BOXZ, g.rdx);
         acc += -s_vz_a[bj] * ea * dt * (-bAj * bAj * 0.5f);
       }
     }
     if (x - 1 >= g.xi0) {
-      const int bj = b - kBoxZ;
+      const int bj = b - BOXZ;
       const float bBj = m.bycB[i - ldz];
-      const float eb = sdm(s_sxz, bj, 1, g.rdz) + sdp(s_sxx, bj, kBoxZ, g.rdx);
+      const float eb = sdm(s_sxz, bj, 1, g.rdz) + sdp(s_sxx, bj, BOXZ, g.rdx);
       acc += -s_vx_a[bj] * eb * dt * (-bBj * bBj * 0.5f);
     }
     gr.den[i] = acc;
   }
+  };
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (z + r < g.nz) cell(z + r, i + r, b + r);
 }
 
 // ---------------------------------------------------------------------------
@@ -736,90 +750,146 @@ __device__ __forceinline__ void fwd_velocity_fast2(const SweepPack<K>& P, int sh
   }
 }
 
-template <int TX, int K>
+// Own-cell values of a thread's R adjacent depths (8-byte paired when R == 2:
+// even depth, ldz a multiple of 32).
+template <int R>
+__device__ __forceinline__ void ldr(const float* p, float (&v)[R]) {
+  if constexpr (R == 2) {
+    const float2 t = ld2(p);
+    v[0] = t.x;
+    v[1] = t.y;
+  } else {
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = p[r];
+  }
+}
+template <int R>
+__device__ __forceinline__ void str(float* p, const float (&v)[R]) {
+  if constexpr (R == 2) {
+    st2(p, v[0], v[1]);
+  } else {
+#pragma unroll
+    for (int r = 0; r < R; ++r) p[r] = v[r];
+  }
+}
+
+// Backward fast bodies, R adjacent depths per thread (tiles of 32 R rows):
+// the own-cell operands of all R depths are loaded before the staged tiles
+// are awaited; the depths are then computed in turn (the stencil samples
+// two depths share are read once after unrolling).
+template <int TX, int K, int R>
 __device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
-  SWEEP_FAST_SLOT(kTileZ)
-  SWEEP_STAGE(5, kBoxZ, 1)
+  constexpr int TZ = 32 * R, BOXZ = TZ + 8;
+  SWEEP_FAST_SLOT(TZ)
+  SWEEP_STAGE(5, BOXZ, R)
   const Grads& gr = S.gr;
   const int it = S.nSteps - 2 - j;
   const float dt = g.dt;
-  float szz = f.szz[i], sxx = f.sxx[i], sxz = f.sxz[i];
-  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
-  const float gl = gr.lam[i], gm = gr.mu[i], w = m.muw[i], h = m.hs[i];
-  const float va_z = f.vz_a[i], va_x = f.vx_a[i];
-  const float hz = m.hs[i - 1], hx = m.hs[i - ldz], hzx = m.hs[i - ldz - 1];
+  float szz[R], sxx[R], sxz[R], lam[R], l2m[R], amu[R], gl[R], gm[R], w[R], h[R], va_z[R], va_x[R], hx[R];
+  ldr<R>(f.szz + i, szz);
+  ldr<R>(f.sxx + i, sxx);
+  ldr<R>(f.sxz + i, sxz);
+  ldr<R>(m.lam + i, lam);
+  ldr<R>(m.l2m + i, l2m);
+  ldr<R>(m.aveMu + i, amu);
+  ldr<R>(gr.lam + i, gl);
+  ldr<R>(gr.mu + i, gm);
+  ldr<R>(m.muw + i, w);
+  ldr<R>(m.hs + i, h);
+  ldr<R>(f.vz_a + i, va_z);
+  ldr<R>(f.vx_a + i, va_x);
+  ldr<R>(m.hs + i - ldz, hx);
+  const float hz0 = m.hs[i - 1], hzx0 = m.hs[i - ldz - 1];
   if (!stage_wait(&bar, err)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
   const float* s_szz_a = sm + 2 * N;
   const float* s_sxx_a = sm + 3 * N;
   const float* s_sxz_a = sm + 4 * N;
-  if (special && z == sh.src_z && x == sh.src_x) {
-    szz -= sh.src_szz_r[it];
-    sxx -= sh.src_sxx_r[it];
+  float o_gl[R], o_gm[R], o_szz[R], o_sxx[R], o_sxz[R], o_vza[R], o_vxa[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int bb = b + r;
+    const float hz = r == 0 ? hz0 : h[r - 1];     // hs at (z-1, x)
+    const float hzx = r == 0 ? hzx0 : hx[r - 1];  // hs at (z-1, x-1)
+    if (special && z + r == sh.src_z && x == sh.src_x) {
+      szz[r] -= sh.src_szz_r[it];
+      sxx[r] -= sh.src_sxx_r[it];
+    }
+    const float dvz_dz = sdm(s_vz, bb, 1, g.rdz);
+    const float dvx_dx = sdm(s_vx, bb, BOXZ, g.rdx);
+    const float dvx_dz = sdp(s_vx, bb, 1, g.rdz);
+    const float dvz_dx = sdp(s_vz, bb, BOXZ, g.rdx);
+    o_szz[r] = szz[r] - (l2m[r] * dvz_dz + lam[r] * dvx_dx) * dt;
+    o_sxx[r] = sxx[r] - (lam[r] * dvz_dz + l2m[r] * dvx_dx) * dt;
+    const float e_own = dvx_dz + dvz_dx;
+    o_sxz[r] = sxz[r] - amu[r] * e_own * dt;
+    const float sa = s_szz_a[bb], xa = s_sxx_a[bb];
+    o_gl[r] = gl[r] + -(sa + xa) * (dvz_dz + dvx_dx) * dt * kMega;
+    const float gmu_own = (-2.0f * sa * dvz_dz * dt - 2.0f * xa * dvx_dx * dt) * kMega;
+    // mu kernel: own term and the three neighbouring 2x2 blocks (all guards hold).
+    float acc = gm[r] + gmu_own;
+    if (h[r] != 0.0f) acc += w[r] * (-s_sxz_a[bb] * e_own * dt * h[r]);
+    if (hz != 0.0f) {
+      const int bj = bb - 1;
+      acc += w[r] * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, BOXZ, g.rdx)) * dt * hz);
+    }
+    if (hx[r] != 0.0f) {
+      const int bj = bb - BOXZ;
+      acc += w[r] * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, BOXZ, g.rdx)) * dt * hx[r]);
+    }
+    if (hzx != 0.0f) {
+      const int b2 = bb - BOXZ - 1;
+      acc += w[r] * (-s_sxz_a[b2] * (sdp(s_vx, b2, 1, g.rdz) + sdp(s_vz, b2, BOXZ, g.rdx)) * dt * hzx);
+    }
+    o_gm[r] = acc;
+    // el_velocity_adj without the psi memory terms.
+    {
+      const float dszz_dx = -sdp(s_szz_a, bb, BOXZ, g.rdx);
+      const float dsxx_dx = -sdp(s_sxx_a, bb, BOXZ, g.rdx);
+      const float dsxz_dz = -sdm(s_sxz_a, bb, 1, g.rdz);
+      o_vxa[r] = va_x[r] + (lam[r] * dszz_dx * dt + l2m[r] * dsxx_dx * dt + amu[r] * dsxz_dz * dt);
+    }
+    {
+      const float dszz_dz = -sdp(s_szz_a, bb, 1, g.rdz);
+      const float dsxx_dz = -sdp(s_sxx_a, bb, 1, g.rdz);
+      const float dsxz_dx = -sdm(s_sxz_a, bb, BOXZ, g.rdx);
+      o_vza[r] = va_z[r] + (l2m[r] * dszz_dz * dt + lam[r] * dsxx_dz * dt + amu[r] * dsxz_dx * dt);
+    }
   }
-  const float dvz_dz = sdm(s_vz, b, 1, g.rdz);
-  const float dvx_dx = sdm(s_vx, b, kBoxZ, g.rdx);
-  const float dvx_dz = sdp(s_vx, b, 1, g.rdz);
-  const float dvz_dx = sdp(s_vz, b, kBoxZ, g.rdx);
-  szz -= (l2m * dvz_dz + lam * dvx_dx) * dt;
-  sxx -= (lam * dvz_dz + l2m * dvx_dx) * dt;
-  const float e_own = dvx_dz + dvz_dx;
-  sxz -= amu * e_own * dt;
-  const float sa = s_szz_a[b], xa = s_sxx_a[b];
-  gr.lam[i] = gl + -(sa + xa) * (dvz_dz + dvx_dx) * dt * kMega;
-  const float gmu_own = (-2.0f * sa * dvz_dz * dt - 2.0f * xa * dvx_dx * dt) * kMega;
-  f.szz[i] = szz;
-  f.sxx[i] = sxx;
-  f.sxz[i] = sxz;
-  // mu kernel: own term and the three neighbouring 2x2 blocks (all guards hold).
-  float acc = gm + gmu_own;
-  if (h != 0.0f) acc += w * (-s_sxz_a[b] * e_own * dt * h);
-  if (hz != 0.0f) {
-    const int bj = b - 1;
-    acc += w * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, kBoxZ, g.rdx)) * dt * hz);
-  }
-  if (hx != 0.0f) {
-    const int bj = b - kBoxZ;
-    acc += w * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, kBoxZ, g.rdx)) * dt * hx);
-  }
-  if (hzx != 0.0f) {
-    const int b2 = b - kBoxZ - 1;
-    acc += w * (-s_sxz_a[b2] * (sdp(s_vx, b2, 1, g.rdz) + sdp(s_vz, b2, kBoxZ, g.rdx)) * dt * hzx);
-  }
-  gr.mu[i] = acc;
-  // el_velocity_adj without the psi memory terms.
-  {
-    const float dszz_dx = -sdp(s_szz_a, b, kBoxZ, g.rdx);
-    const float dsxx_dx = -sdp(s_sxx_a, b, kBoxZ, g.rdx);
-    const float dsxz_dz = -sdm(s_sxz_a, b, 1, g.rdz);
-    f.vx_a[i] = va_x + (lam * dszz_dx * dt + l2m * dsxx_dx * dt + amu * dsxz_dz * dt);
-  }
-  {
-    const float dszz_dz = -sdp(s_szz_a, b, 1, g.rdz);
-    const float dsxx_dz = -sdp(s_sxx_a, b, 1, g.rdz);
-    const float dsxz_dx = -sdm(s_sxz_a, b, kBoxZ, g.rdx);
-    f.vz_a[i] = va_z + (l2m * dszz_dz * dt + lam * dsxx_dz * dt + amu * dsxz_dx * dt);
-  }
+  str<R>(gr.lam + i, o_gl);
+  str<R>(f.szz + i, o_szz);
+  str<R>(f.sxx + i, o_sxx);
+  str<R>(f.sxz + i, o_sxz);
+  str<R>(gr.mu + i, o_gm);
+  str<R>(f.vx_a + i, o_vxa);
+  str<R>(f.vz_a + i, o_vza);
 }
 
-template <int TX, int K>
+template <int TX, int K, int R>
 __device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
-  SWEEP_FAST_SLOT(kTileZ)
-  SWEEP_STAGE(5, kBoxZ, 1)
+  constexpr int TZ = 32 * R, BOXZ = TZ + 8;
+  SWEEP_FAST_SLOT(TZ)
+  SWEEP_STAGE(5, BOXZ, R)
   const Grads& gr = S.gr;
   const int it = S.nSteps - 2 - j;
   const int rev = it >= 1;
   const float dt = g.dt;
-  float sa = f.szz_a[i], xa = f.sxx_a[i], za = f.sxz_a[i];
-  const float bA = m.bycA[i], bB = m.bycB[i];
-  float vz = 0.0f, vx = 0.0f, gd = 0.0f, bAj = 0.0f, bBj = 0.0f;
+  float sa[R], xa[R], za[R], bA[R], bB[R], vz[R], vx[R], gd[R], bBj[R];
+  ldr<R>(f.szz_a + i, sa);
+  ldr<R>(f.sxx_a + i, xa);
+  ldr<R>(f.sxz_a + i, za);
+  ldr<R>(m.bycA + i, bA);
+  ldr<R>(m.bycB + i, bB);
+  float bAj0 = 0.0f;
+#pragma unroll
+  for (int r = 0; r < R; ++r) vz[r] = vx[r] = gd[r] = bBj[r] = 0.0f;
   if (rev) {
-    vz = f.vz[i];
-    vx = f.vx[i];
-    gd = gr.den[i];
-    bAj = m.bycA[i - 1];
-    bBj = m.bycB[i - ldz];
+    ldr<R>(f.vz + i, vz);
+    ldr<R>(f.vx + i, vx);
+    ldr<R>(gr.den + i, gd);
+    ldr<R>(m.bycB + i - ldz, bBj);
+    bAj0 = m.bycA[i - 1];
   }
   if (!stage_wait(&bar, err)) return;
   const float* s_vz_a = sm;
@@ -827,52 +897,278 @@ __device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int 
   const float* s_szz = sm + 2 * N;
   const float* s_sxx = sm + 3 * N;
   const float* s_sxz = sm + 4 * N;
-  if (special) {
-    const int2 rr = bin_range(sh, z, x);
-    for (int k = rr.x; k < rr.y; ++k) {
-      const int r = sh.blk_rec[k];
-      if (sh.rec_z[r] == z && sh.rec_x[r] == x) {
-        const float rv = sh.res[static_cast<size_t>(r) * sh.nSteps + it];
-        sa += rv;
-        xa += 3.0f * rv;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int bb = b + r;
+    if (special) {
+      const int2 rr = bin_range(sh, z + r, x);
+      for (int k = rr.x; k < rr.y; ++k) {
+        const int q = sh.blk_rec[k];
+        if (sh.rec_z[q] == z + r && sh.rec_x[q] == x) {
+          const float rv = sh.res[static_cast<size_t>(q) * sh.nSteps + it];
+          sa[r] += rv;
+          xa[r] += 3.0f * rv;
+        }
+      }
+    }
+    {
+      const float dvz_dx = -sdp(s_vz_a, bb, BOXZ, g.rdx);
+      const float dvx_dz = -sdp(s_vx_a, bb, 1, g.rdz);
+      za[r] += dvz_dx * bA[r] * dt + dvx_dz * bB[r] * dt;
+    }
+    {
+      const float dvx_dx = -sdm(s_vx_a, bb, BOXZ, g.rdx);
+      const float dvz_dz = -sdm(s_vz_a, bb, 1, g.rdz);
+      xa[r] += bB[r] * dvx_dx * dt;
+      sa[r] += bA[r] * dvz_dz * dt;
+    }
+  }
+  str<R>(f.sxz_a + i, za);
+  str<R>(f.szz_a + i, sa);
+  str<R>(f.sxx_a + i, xa);
+  if (!rev) return;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int bb = b + r;
+    if (special && z + r == sh.src_z && x == sh.src_x) sh.gstf[it - 1] = -(sa[r] + 3.0f * xa[r]) * dt;
+    const float ea = sdp(s_szz, bb, 1, g.rdz) + sdm(s_sxz, bb, BOXZ, g.rdx);  // dszz_dz + dsxz_dx
+    const float eb = sdm(s_sxz, bb, 1, g.rdz) + sdp(s_sxx, bb, BOXZ, g.rdx);  // dsxz_dz + dsxx_dx
+    vz[r] = vz[r] - ea * bA[r] * dt;
+    vx[r] = vx[r] - eb * bB[r] * dt;
+    // rho kernel gather (all guards hold).
+    const float bAj = r == 0 ? bAj0 : bA[r - 1];  // bycA at (z-1, x)
+    float acc = gd[r];
+    acc += -s_vz_a[bb] * ea * dt * (-bA[r] * bA[r] * 0.5f);
+    acc += -s_vx_a[bb] * eb * dt * (-bB[r] * bB[r] * 0.5f);
+    {
+      const int bj = bb - 1;
+      const float e = sdp(s_szz, bj, 1, g.rdz) + sdm(s_sxz, bj, BOXZ, g.rdx);
+      acc += -s_vz_a[bj] * e * dt * (-bAj * bAj * 0.5f);
+    }
+    {
+      const int bj = bb - BOXZ;
+      const float e = sdm(s_sxz, bj, 1, g.rdz) + sdp(s_sxx, bj, BOXZ, g.rdx);
+      acc += -s_vx_a[bj] * e * dt * (-bBj[r] * bBj[r] * 0.5f);
+    }
+    gd[r] = acc;
+  }
+  str<R>(f.vz + i, vz);
+  str<R>(f.vx + i, vx);
+  str<R>(gr.den + i, gd);
+}
+
+// Backward fast bodies with two adjacent depths per thread, staged samples
+// read in pairs (as the forward two-row bodies): with b even, the float2 at
+// b + o (o even) holds the depths of both cells at offset o, so a z stencil
+// of both depths takes the pairs at b - 2, b, b + 2 and an x stencil the
+// pairs at b + k BOXZ. Operation order per cell is that of the one-row body.
+template <int TX, int K>
+__device__ __forceinline__ void bwd_B_fast2(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
+  constexpr int TZ = 64, BOXZ = TZ + 8, R = 2;
+  SWEEP_FAST_SLOT(TZ)
+  SWEEP_STAGE(5, BOXZ, R)
+  const Grads& gr = S.gr;
+  const int it = S.nSteps - 2 - j;
+  const float dt = g.dt;
+  float szz[2], sxx[2], sxz[2], lam[2], l2m[2], amu[2], gl[2], gm[2], w[2], h[2], va_z[2], va_x[2], hx[2];
+  ldr<2>(f.szz + i, szz);
+  ldr<2>(f.sxx + i, sxx);
+  ldr<2>(f.sxz + i, sxz);
+  ldr<2>(m.lam + i, lam);
+  ldr<2>(m.l2m + i, l2m);
+  ldr<2>(m.aveMu + i, amu);
+  ldr<2>(gr.lam + i, gl);
+  ldr<2>(gr.mu + i, gm);
+  ldr<2>(m.muw + i, w);
+  ldr<2>(m.hs + i, h);
+  ldr<2>(f.vz_a + i, va_z);
+  ldr<2>(f.vx_a + i, va_x);
+  ldr<2>(m.hs + i - ldz, hx);
+  const float hz0 = m.hs[i - 1], hzx0 = m.hs[i - ldz - 1];
+  if (!stage_wait(&bar, err)) return;
+  const float* s_vz = sm;
+  const float* s_vx = sm + N;
+  const float* s_sza = sm + 2 * N;
+  const float* s_xxa = sm + 3 * N;
+  const float* s_xza = sm + 4 * N;
+  const float rdz = g.rdz, rdx = g.rdx;
+  constexpr int B = BOXZ;
+  // vz: z pairs and x pairs
+  const float2 VZm = ld2(s_vz + b - 2), V0 = ld2(s_vz + b), VZp = ld2(s_vz + b + 2);
+  const float2 Vp1 = ld2(s_vz + b + B), Vp2 = ld2(s_vz + b + 2 * B), Vm1 = ld2(s_vz + b - B),
+               Vm2 = ld2(s_vz + b - 2 * B);
+  // vx: z pairs at columns 0 and -1, x pairs
+  const float2 UZm = ld2(s_vx + b - 2), U0 = ld2(s_vx + b), UZp = ld2(s_vx + b + 2);
+  const float2 Um1 = ld2(s_vx + b - B), Up1 = ld2(s_vx + b + B), Um2 = ld2(s_vx + b - 2 * B);
+  const float2 UmZm = ld2(s_vx + b - B - 2), UmZp = ld2(s_vx + b - B + 2);
+  // depth b - 1 at columns +1, +2, -1, -2 (the mu gathers of the upper cell)
+  const float vz_p1m = s_vz[b + B - 1], vz_p2m = s_vz[b + 2 * B - 1], vz_m1m = s_vz[b - B - 1],
+              vz_m2m = s_vz[b - 2 * B - 1];
+  // own-cell strains
+  const float dvz_dz[2] = {dd(V0.x, VZm.y, V0.y, VZm.x, rdz), dd(V0.y, V0.x, VZp.x, VZm.y, rdz)};
+  const float dvx_dx[2] = {dd(U0.x, Um1.x, Up1.x, Um2.x, rdx), dd(U0.y, Um1.y, Up1.y, Um2.y, rdx)};
+  const float dvx_dz[2] = {dd(U0.y, U0.x, UZp.x, UZm.y, rdz), dd(UZp.x, U0.y, UZp.y, U0.x, rdz)};
+  const float dvz_dx[2] = {dd(Vp1.x, V0.x, Vp2.x, Vm1.x, rdx), dd(Vp1.y, V0.y, Vp2.y, Vm1.y, rdx)};
+  // e = dvx_dz + dvz_dx at (z, x), (z-1, x), (z, x-1), (z-1, x-1) for both depths
+  const float e_own[2] = {dvx_dz[0] + dvz_dx[0], dvx_dz[1] + dvz_dx[1]};
+  const float e_zm0 = dd(U0.x, UZm.y, U0.y, UZm.x, rdz) + dd(vz_p1m, VZm.y, vz_p2m, vz_m1m, rdx);
+  const float e_xm[2] = {dd(Um1.y, Um1.x, UmZp.x, UmZm.y, rdz) + dd(V0.x, Vm1.x, Vp1.x, Vm2.x, rdx),
+                         dd(UmZp.x, Um1.y, UmZp.y, Um1.x, rdz) + dd(V0.y, Vm1.y, Vp1.y, Vm2.y, rdx)};
+  const float e_zxm0 = dd(Um1.x, UmZm.y, Um1.y, UmZm.x, rdz) + dd(VZm.y, vz_m1m, vz_p1m, vz_m2m, rdx);
+  const float e_zm[2] = {e_zm0, e_own[0]};
+  const float e_zxm[2] = {e_zxm0, e_xm[0]};
+  // adjoint stresses
+  const float2 SA0 = ld2(s_sza + b), SAZm = ld2(s_sza + b - 2), SAZp = ld2(s_sza + b + 2);
+  const float2 SAp1 = ld2(s_sza + b + B), SAp2 = ld2(s_sza + b + 2 * B), SAm1 = ld2(s_sza + b - B);
+  const float2 XA0 = ld2(s_xxa + b), XAZm = ld2(s_xxa + b - 2), XAZp = ld2(s_xxa + b + 2);
+  const float2 XAp1 = ld2(s_xxa + b + B), XAp2 = ld2(s_xxa + b + 2 * B), XAm1 = ld2(s_xxa + b - B);
+  const float2 ZA0 = ld2(s_xza + b), ZAZm = ld2(s_xza + b - 2), ZAZp = ld2(s_xza + b + 2);
+  const float2 ZAm1 = ld2(s_xza + b - B), ZAp1 = ld2(s_xza + b + B), ZAm2 = ld2(s_xza + b - 2 * B);
+  const float2 ZAmZm = ld2(s_xza + b - B - 2);
+  const float sa_[2] = {SA0.x, SA0.y}, xa_[2] = {XA0.x, XA0.y};
+  const float za_own[2] = {ZA0.x, ZA0.y}, za_zm[2] = {ZAZm.y, ZA0.x};
+  const float za_xm[2] = {ZAm1.x, ZAm1.y}, za_zxm[2] = {ZAmZm.y, ZAm1.x};
+  const float dszz_dx[2] = {-dd(SAp1.x, SA0.x, SAp2.x, SAm1.x, rdx), -dd(SAp1.y, SA0.y, SAp2.y, SAm1.y, rdx)};
+  const float dsxx_dx[2] = {-dd(XAp1.x, XA0.x, XAp2.x, XAm1.x, rdx), -dd(XAp1.y, XA0.y, XAp2.y, XAm1.y, rdx)};
+  const float dsxz_dz[2] = {-dd(ZA0.x, ZAZm.y, ZA0.y, ZAZm.x, rdz), -dd(ZA0.y, ZA0.x, ZAZp.x, ZAZm.y, rdz)};
+  const float dszz_dz[2] = {-dd(SA0.y, SA0.x, SAZp.x, SAZm.y, rdz), -dd(SAZp.x, SA0.y, SAZp.y, SA0.x, rdz)};
+  const float dsxx_dz[2] = {-dd(XA0.y, XA0.x, XAZp.x, XAZm.y, rdz), -dd(XAZp.x, XA0.y, XAZp.y, XA0.x, rdz)};
+  const float dsxz_dx[2] = {-dd(ZA0.x, ZAm1.x, ZAp1.x, ZAm2.x, rdx), -dd(ZA0.y, ZAm1.y, ZAp1.y, ZAm2.y, rdx)};
+  float o_gl[2], o_gm[2], o_szz[2], o_sxx[2], o_sxz[2], o_vza[2], o_vxa[2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const float hz = r == 0 ? hz0 : h[0];
+    const float hzx = r == 0 ? hzx0 : hx[0];
+    if (special && z + r == sh.src_z && x == sh.src_x) {
+      szz[r] -= sh.src_szz_r[it];
+      sxx[r] -= sh.src_sxx_r[it];
+    }
+    o_szz[r] = szz[r] - (l2m[r] * dvz_dz[r] + lam[r] * dvx_dx[r]) * dt;
+    o_sxx[r] = sxx[r] - (lam[r] * dvz_dz[r] + l2m[r] * dvx_dx[r]) * dt;
+    o_sxz[r] = sxz[r] - amu[r] * e_own[r] * dt;
+    o_gl[r] = gl[r] + -(sa_[r] + xa_[r]) * (dvz_dz[r] + dvx_dx[r]) * dt * kMega;
+    const float gmu_own = (-2.0f * sa_[r] * dvz_dz[r] * dt - 2.0f * xa_[r] * dvx_dx[r] * dt) * kMega;
+    float acc = gm[r] + gmu_own;
+    if (h[r] != 0.0f) acc += w[r] * (-za_own[r] * e_own[r] * dt * h[r]);
+    if (hz != 0.0f) acc += w[r] * (-za_zm[r] * e_zm[r] * dt * hz);
+    if (hx[r] != 0.0f) acc += w[r] * (-za_xm[r] * e_xm[r] * dt * hx[r]);
+    if (hzx != 0.0f) acc += w[r] * (-za_zxm[r] * e_zxm[r] * dt * hzx);
+    o_gm[r] = acc;
+    o_vxa[r] = va_x[r] + (lam[r] * dszz_dx[r] * dt + l2m[r] * dsxx_dx[r] * dt + amu[r] * dsxz_dz[r] * dt);
+    o_vza[r] = va_z[r] + (l2m[r] * dszz_dz[r] * dt + lam[r] * dsxx_dz[r] * dt + amu[r] * dsxz_dx[r] * dt);
+  }
+  str<2>(gr.lam + i, o_gl);
+  str<2>(f.szz + i, o_szz);
+  str<2>(f.sxx + i, o_sxx);
+  str<2>(f.sxz + i, o_sxz);
+  str<2>(gr.mu + i, o_gm);
+  str<2>(f.vx_a + i, o_vxa);
+  str<2>(f.vz_a + i, o_vza);
+}
+
+template <int TX, int K>
+__device__ __forceinline__ void bwd_C_fast2(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
+  constexpr int TZ = 64, BOXZ = TZ + 8, R = 2;
+  SWEEP_FAST_SLOT(TZ)
+  SWEEP_STAGE(5, BOXZ, R)
+  const Grads& gr = S.gr;
+  const int it = S.nSteps - 2 - j;
+  const int rev = it >= 1;
+  const float dt = g.dt;
+  float sa[2], xa[2], za[2], bA[2], bB[2], vz[2], vx[2], gd[2], bBj[2];
+  ldr<2>(f.szz_a + i, sa);
+  ldr<2>(f.sxx_a + i, xa);
+  ldr<2>(f.sxz_a + i, za);
+  ldr<2>(m.bycA + i, bA);
+  ldr<2>(m.bycB + i, bB);
+  float bAj0 = 0.0f;
+  vz[0] = vz[1] = vx[0] = vx[1] = gd[0] = gd[1] = bBj[0] = bBj[1] = 0.0f;
+  if (rev) {
+    ldr<2>(f.vz + i, vz);
+    ldr<2>(f.vx + i, vx);
+    ldr<2>(gr.den + i, gd);
+    ldr<2>(m.bycB + i - ldz, bBj);
+    bAj0 = m.bycA[i - 1];
+  }
+  if (!stage_wait(&bar, err)) return;
+  const float* s_vza = sm;
+  const float* s_vxa = sm + N;
+  const float* s_szz = sm + 2 * N;
+  const float* s_sxx = sm + 3 * N;
+  const float* s_sxz = sm + 4 * N;
+  const float rdz = g.rdz, rdx = g.rdx;
+  constexpr int B = BOXZ;
+  const float2 VA0 = ld2(s_vza + b), VAZm = ld2(s_vza + b - 2), VAZp = ld2(s_vza + b + 2);
+  const float2 VAp1 = ld2(s_vza + b + B), VAp2 = ld2(s_vza + b + 2 * B), VAm1 = ld2(s_vza + b - B);
+  const float2 XA0 = ld2(s_vxa + b), XAZm = ld2(s_vxa + b - 2), XAZp = ld2(s_vxa + b + 2);
+  const float2 XAm1 = ld2(s_vxa + b - B), XAp1 = ld2(s_vxa + b + B), XAm2 = ld2(s_vxa + b - 2 * B);
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    if (special) {
+      const int2 rr = bin_range(sh, z + r, x);
+      for (int k = rr.x; k < rr.y; ++k) {
+        const int q = sh.blk_rec[k];
+        if (sh.rec_z[q] == z + r && sh.rec_x[q] == x) {
+          const float rv = sh.res[static_cast<size_t>(q) * sh.nSteps + it];
+          sa[r] += rv;
+          xa[r] += 3.0f * rv;
+        }
       }
     }
   }
   {
-    const float dvz_dx = -sdp(s_vz_a, b, kBoxZ, g.rdx);
-    const float dvx_dz = -sdp(s_vx_a, b, 1, g.rdz);
-    za += dvz_dx * bA * dt + dvx_dz * bB * dt;
-    f.sxz_a[i] = za;
+    const float dvz_dx[2] = {-dd(VAp1.x, VA0.x, VAp2.x, VAm1.x, rdx), -dd(VAp1.y, VA0.y, VAp2.y, VAm1.y, rdx)};
+    const float dvx_dz[2] = {-dd(XA0.y, XA0.x, XAZp.x, XAZm.y, rdz), -dd(XAZp.x, XA0.y, XAZp.y, XA0.x, rdz)};
+    const float dvx_dx[2] = {-dd(XA0.x, XAm1.x, XAp1.x, XAm2.x, rdx), -dd(XA0.y, XAm1.y, XAp1.y, XAm2.y, rdx)};
+    const float dvz_dz[2] = {-dd(VA0.x, VAZm.y, VA0.y, VAZm.x, rdz), -dd(VA0.y, VA0.x, VAZp.x, VAZm.y, rdz)};
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      za[r] += dvz_dx[r] * bA[r] * dt + dvx_dz[r] * bB[r] * dt;
+      xa[r] += bB[r] * dvx_dx[r] * dt;
+      sa[r] += bA[r] * dvz_dz[r] * dt;
+    }
   }
-  {
-    const float dvx_dx = -sdm(s_vx_a, b, kBoxZ, g.rdx);
-    const float dvz_dz = -sdm(s_vz_a, b, 1, g.rdz);
-    xa += bB * dvx_dx * dt;
-    sa += bA * dvz_dz * dt;
-  }
-  f.szz_a[i] = sa;
-  f.sxx_a[i] = xa;
+  str<2>(f.sxz_a + i, za);
+  str<2>(f.szz_a + i, sa);
+  str<2>(f.sxx_a + i, xa);
   if (!rev) return;
-  if (special && z == sh.src_z && x == sh.src_x) sh.gstf[it - 1] = -(sa + 3.0f * xa) * dt;
-  const float ea = sdp(s_szz, b, 1, g.rdz) + sdm(s_sxz, b, kBoxZ, g.rdx);  // dszz_dz + dsxz_dx
-  const float eb = sdm(s_sxz, b, 1, g.rdz) + sdp(s_sxx, b, kBoxZ, g.rdx);  // dsxz_dz + dsxx_dx
-  f.vz[i] = vz - ea * bA * dt;
-  f.vx[i] = vx - eb * bB * dt;
-  // rho kernel gather (all guards hold).
-  float acc = gd;
-  acc += -s_vz_a[b] * ea * dt * (-bA * bA * 0.5f);
-  acc += -s_vx_a[b] * eb * dt * (-bB * bB * 0.5f);
-  {
-    const int bj = b - 1;
-    const float e = sdp(s_szz, bj, 1, g.rdz) + sdm(s_sxz, bj, kBoxZ, g.rdx);
-    acc += -s_vz_a[bj] * e * dt * (-bAj * bAj * 0.5f);
+  const float2 PZm = ld2(s_szz + b - 2), PZ0 = ld2(s_szz + b), PZp = ld2(s_szz + b + 2);
+  const float2 Q0 = ld2(s_sxz + b), Qm1 = ld2(s_sxz + b - B), Qp1 = ld2(s_sxz + b + B), Qm2 = ld2(s_sxz + b - 2 * B);
+  const float2 QZm = ld2(s_sxz + b - 2), QZp = ld2(s_sxz + b + 2);
+  const float2 QmZm = ld2(s_sxz + b - B - 2), QmZp = ld2(s_sxz + b - B + 2);
+  const float2 X0 = ld2(s_sxx + b), Xp1 = ld2(s_sxx + b + B), Xp2 = ld2(s_sxx + b + 2 * B), Xm1 = ld2(s_sxx + b - B),
+               Xm2 = ld2(s_sxx + b - 2 * B);
+  // sxz at depth b - 1, columns -1, +1, -2 (the upper cell's z-neighbour gather)
+  const float q_m1m = s_sxz[b - B - 1], q_p1m = s_sxz[b + B - 1], q_m2m = s_sxz[b - 2 * B - 1];
+  // ea = dszz_dz + dsxz_dx, eb = dsxz_dz + dsxx_dx at (z, x) for both depths
+  const float ea[2] = {dd(PZ0.y, PZ0.x, PZp.x, PZm.y, rdz) + dd(Q0.x, Qm1.x, Qp1.x, Qm2.x, rdx),
+                       dd(PZp.x, PZ0.y, PZp.y, PZ0.x, rdz) + dd(Q0.y, Qm1.y, Qp1.y, Qm2.y, rdx)};
+  const float eb[2] = {dd(Q0.x, QZm.y, Q0.y, QZm.x, rdz) + dd(Xp1.x, X0.x, Xp2.x, Xm1.x, rdx),
+                       dd(Q0.y, Q0.x, QZp.x, QZm.y, rdz) + dd(Xp1.y, X0.y, Xp2.y, Xm1.y, rdx)};
+  // ea at (z-1, x): the upper cell's from depth b - 1, the lower cell's is ea[0]
+  const float ea_zm0 = dd(PZ0.x, PZm.y, PZ0.y, PZm.x, rdz) + dd(QZm.y, q_m1m, q_p1m, q_m2m, rdx);
+  // eb at (z, x-1)
+  const float eb_xm[2] = {dd(Qm1.x, QmZm.y, Qm1.y, QmZm.x, rdz) + dd(X0.x, Xm1.x, Xp1.x, Xm2.x, rdx),
+                          dd(Qm1.y, Qm1.x, QmZp.x, QmZm.y, rdz) + dd(X0.y, Xm1.y, Xp1.y, Xm2.y, rdx)};
+  const float ea_zm[2] = {ea_zm0, ea[0]};
+  const float va_own[2] = {VA0.x, VA0.y}, va_zm[2] = {VAZm.y, VA0.x};
+  const float xa_own[2] = {XA0.x, XA0.y}, xa_xm[2] = {XAm1.x, XAm1.y};
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    if (special && z + r == sh.src_z && x == sh.src_x) sh.gstf[it - 1] = -(sa[r] + 3.0f * xa[r]) * dt;
+    vz[r] = vz[r] - ea[r] * bA[r] * dt;
+    vx[r] = vx[r] - eb[r] * bB[r] * dt;
+    const float bAj = r == 0 ? bAj0 : bA[0];
+    float acc = gd[r];
+    acc += -va_own[r] * ea[r] * dt * (-bA[r] * bA[r] * 0.5f);
+    acc += -xa_own[r] * eb[r] * dt * (-bB[r] * bB[r] * 0.5f);
+    acc += -va_zm[r] * ea_zm[r] * dt * (-bAj * bAj * 0.5f);
+    acc += -xa_xm[r] * eb_xm[r] * dt * (-bBj[r] * bBj[r] * 0.5f);
+    gd[r] = acc;
   }
-  {
-    const int bj = b - kBoxZ;
-    const float e = sdm(s_sxz, bj, 1, g.rdz) + sdp(s_sxx, bj, kBoxZ, g.rdx);
-    acc += -s_vx_a[bj] * e * dt * (-bBj * bBj * 0.5f);
-  }
-  gr.den[i] = acc;
+  str<2>(f.vz + i, vz);
+  str<2>(f.vx + i, vx);
+  str<2>(gr.den + i, gd);
 }
 
 // ---------------------------------------------------------------------------
@@ -906,22 +1202,31 @@ __global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ SweepPack<K> P
   }
 }
 
-template <int TX, int K>
+// Backward sweeps: R depths per thread (tiles of 32 R rows), R in {1, 2}.
+template <int TX, int K, int R>
 __global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
-  SWEEP_KERNEL_TILE(kTileZ)
-  if (fast)
-    bwd_B_fast<TX, K>(P, shot, z0, x0, j, err);
-  else
-    bwd_B_edge<TX, K>(P, shot, z0, x0, j, err);
+  SWEEP_KERNEL_TILE(32 * R)
+  if (fast) {
+    if constexpr (R == 1)
+      bwd_B_fast<TX, K, 1>(P, shot, z0, x0, j, err);
+    else
+      bwd_B_fast2<TX, K>(P, shot, z0, x0, j, err);
+  } else {
+    bwd_B_edge<TX, K, R>(P, shot, z0, x0, j, err);
+  }
 }
 
-template <int TX, int K>
+template <int TX, int K, int R>
 __global__ void BWD_BOUNDS k_bwd_C(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
-  SWEEP_KERNEL_TILE(kTileZ)
-  if (fast)
-    bwd_C_fast<TX, K>(P, shot, z0, x0, j, err);
-  else
-    bwd_C_edge<TX, K>(P, shot, z0, x0, j, err);
+  SWEEP_KERNEL_TILE(32 * R)
+  if (fast) {
+    if constexpr (R == 1)
+      bwd_C_fast<TX, K, 1>(P, shot, z0, x0, j, err);
+    else
+      bwd_C_fast2<TX, K>(P, shot, z0, x0, j, err);
+  } else {
+    bwd_C_edge<TX, K, R>(P, shot, z0, x0, j, err);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1369,18 +1674,26 @@ int launch_fwd_velocity(cudaStream_t s, int tx, int rows, const SweepPack<K>& p,
 }
 
 template <int K>
-int launch_bwd_B(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
+int launch_bwd_B(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
-                                   smem_bytes<TX, kBoxZ>(5), s, p, j, err))
+  if (rows == 2)
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
+                                     smem_bytes<TX, kBoxZFwd>(5), s, p, j, err))
+  else
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+                                     smem_bytes<TX, kBoxZ>(5), s, p, j, err))
   return 1;
 }
 
 template <int K>
-int launch_bwd_C(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
+int launch_bwd_C(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err) {
-  FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, K>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
-                                   smem_bytes<TX, kBoxZ>(5), s, p, j, err))
+  if (rows == 2)
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, K, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
+                                     smem_bytes<TX, kBoxZFwd>(5), s, p, j, err))
+  else
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, K, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+                                     smem_bytes<TX, kBoxZ>(5), s, p, j, err))
   return 1;
 }
 
@@ -1389,15 +1702,17 @@ int launch_bwd_C(cudaStream_t s, int tx, const SweepPack<K>& p, int nshots, cons
                                     unsigned*);                                                                  \
   template int launch_fwd_velocity<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&,        \
                                       unsigned*);                                                                \
-  template int launch_bwd_B<K>(cudaStream_t, int, const SweepPack<K>&, int, const SweepGrid&, int, unsigned*);   \
-  template int launch_bwd_C<K>(cudaStream_t, int, const SweepPack<K>&, int, const SweepGrid&, int, unsigned*);
+  template int launch_bwd_B<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&, int,           \
+                               unsigned*);                                                                       \
+  template int launch_bwd_C<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&, int,           \
+                               unsigned*);
 FWIGB_INSTANTIATE(1)
 FWIGB_INSTANTIATE(kPackShots)
 #undef FWIGB_INSTANTIATE
 
 // Tensor maps: one per staged array, a 2-D view (z inner, x outer; row stride
 // ldz floats) with the box kBoxZ x (TX + 4), and kBoxZFwd x (TX + 4) for
-// the two-row forward sweeps. cuTensorMapEncodeTiled checks the
+// the two-row sweeps. cuTensorMapEncodeTiled checks the
 // base (16-byte aligned: every array starts a multiple of ldz*nx floats into
 // a 256-byte aligned allocation) and the stride (ldz*4, a multiple of 128);
 // the x coordinate of every copy, z0 - 4 with z0 a multiple of 32, is a
@@ -1440,6 +1755,10 @@ bool encode_sweep_maps(const Geo& g, const Fields& f, int tx, SweepMaps& out, co
        one(&out.b.t[3], f.sxx_a, B) && one(&out.b.t[4], f.sxz_a, B);
   ok = ok && one(&out.c.t[0], f.vz_a, B) && one(&out.c.t[1], f.vx_a, B) && one(&out.c.t[2], f.szz, B) &&
        one(&out.c.t[3], f.sxx, B) && one(&out.c.t[4], f.sxz, B);
+  ok = ok && one(&out.bw.t[0], f.vz, F) && one(&out.bw.t[1], f.vx, F) && one(&out.bw.t[2], f.szz_a, F) &&
+       one(&out.bw.t[3], f.sxx_a, F) && one(&out.bw.t[4], f.sxz_a, F);
+  ok = ok && one(&out.cw.t[0], f.vz_a, F) && one(&out.cw.t[1], f.vx_a, F) && one(&out.cw.t[2], f.szz, F) &&
+       one(&out.cw.t[3], f.sxx, F) && one(&out.cw.t[4], f.sxz, F);
   if (!ok) *err = "cuTensorMapEncodeTiled rejected a sweep tile";
   return ok;
 }

@@ -217,6 +217,11 @@ class FwiContext:
         t = None if widths is None else np.ascontiguousarray(widths, dtype=np.int32)
         _lib.check(self._lib.fwigb_set_tile_config(self._h, _lib.iptr(t)), self._h)
 
+    def set_tile_rows(self, rows) -> None:
+        """Fix the depths per thread (1 or 2) of the four sweeps."""
+        t = np.ascontiguousarray(rows, dtype=np.int32)
+        _lib.check(self._lib.fwigb_set_tile_rows(self._h, _lib.iptr(t)), self._h)
+
     def set_graphs(self, enable: bool) -> None:
         """Replay a lone shot's launch sequence from a CUDA graph (default on)."""
         _lib.check(self._lib.fwigb_set_graphs(self._h, int(enable)), self._h)

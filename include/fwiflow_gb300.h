@@ -164,13 +164,15 @@ int fwigb_fetch_illumination(fwigb_ctx *ctx, double *illum);
 
 /* Tile widths (columns per thread block: 4, 8 or 16) of the four sweeps
  * (forward stress, forward velocity, backward B, backward C). By default an
- * autotuner times every width (and, for the forward sweeps, 1 or 2 depths per
- * thread) on the context's grid at the first run and keeps the fastest;
- * fwigb_set_tile_config fixes the widths (NULL re-enables tuning).
+ * autotuner times every width and 1 or 2 depths per thread on the context's
+ * grid at the first run and keeps the fastest; fwigb_set_tile_config fixes
+ * the widths (NULL re-enables tuning), fwigb_set_tile_rows the depths per
+ * thread (1 or 2 each; it also stops the tuning).
  * fwigb_tile_rows gives the depths per thread of the four sweeps. */
 int fwigb_tile_config(const fwigb_ctx *ctx, int *tile_x);
 int fwigb_set_tile_config(fwigb_ctx *ctx, const int *tile_x);
 int fwigb_tile_rows(const fwigb_ctx *ctx, int *rows);
+int fwigb_set_tile_rows(fwigb_ctx *ctx, const int *rows);
 
 /* CUDA graphs (on by default): a run whose shots form a single group of one
  * shot records its whole launch sequence (about 4 launches per time step) into a

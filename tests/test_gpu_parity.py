@@ -75,6 +75,66 @@ def test_cuda_matches_reference_golden_small_layered(gpu_lib, fw, tmp_path):
     ctx.close()
 
 
+@pytest.mark.parametrize("width", [4, 8, 16])
+@pytest.mark.parametrize("rows", [1, 2])
+def test_every_tile_shape_matches_reference_golden(width, rows, gpu_lib, fw, tmp_path):
+    """Each tile shape the autotuner may pick (width 4 / 8 / 16 columns, 1 or
+    2 depths per thread), fixed for all four sweeps, on the 100x200 golden
+    workload: a two-shot call (16-shot parameter packs) against the
+    reference's gathers, misfit and gradients, and a one-shot call (one-shot
+    packs) against the reference's wavelet gradient of that shot."""
+    d, w, para, _ = golden_workload("small_layered", tmp_path)
+    s = int(d["stride"])
+    ctx = fw.FwiContext(para, 0)
+    ctx.set_tile_config([width] * 4)
+    ctx.set_tile_rows([rows] * 4)
+    g = np.stack(ctx.obs(*w.moduli(w.vp_obs), w.stf, [0, 1], write_files=True))
+    assert ctx.tile_config() == [width] * 4 and ctx.tile_rows() == [rows] * 4
+    assert rel(g.reshape(-1)[::s], d["gathers_sub"]) < TOL_DATA
+    J, gl, gm, gd, gs = ctx.misfit_grad(*w.moduli(), w.stf, [0, 1])
+    assert abs(J - float(d["misfit"])) <= TOL_DATA * abs(float(d["misfit"]))
+    for k, a in (("g_lambda", gl), ("g_mu", gm), ("g_den", gd)):
+        assert rel(a.reshape(-1)[::s], d[k + "_sub"]) < TOL_GRAD, k
+    assert rel(gs, d["g_stf"]) < TOL_GRAD
+    _, _, _, _, gs1 = ctx.misfit_grad(*w.moduli(), w.stf, [0])
+    assert rel(gs1[0], d["g_stf"][0]) < TOL_GRAD
+    ctx.close()
+
+
+def test_every_tile_shape_with_deep_source_and_receivers(gpu_lib, fw, orc, tmp_path):
+    """Source and receivers deep inside the grid, so that they fall in tiles
+    away from the CPML and ring (the fast tile bodies' source, receiver and
+    wavelet-gradient terms): every tile shape against the oracle."""
+    from fwiflow_gb300 import synthetic
+
+    w = synthetic.tiny(nz=120, nx=160, nPml=12, nSteps=150, n_shots=2, seed=6)
+    for k, s in enumerate(w.shots):
+        xr = list(range(10, 150, 3)) + [80 + 7 * k] * 20
+        zr = [70] * len(range(10, 150, 3)) + list(range(20, 100, 4))
+        s["x_rec"], s["z_rec"] = xr, zr
+        s["z_src"], s["x_src"] = 60 + 5 * k, 70 + 20 * k
+    para = w.write_files(str(tmp_path))
+    ids = [0, 1]
+    lo, mo, ro = w.moduli(w.vp_obs)
+    ref = orc.cufd(2, lo, mo, ro, w.stf, ids, para, write_files=True, want_gathers=True)["gathers"]
+    lam, mu, rho = w.moduli()
+    r1 = orc.cufd(1, lam, mu, rho, w.stf, ids, para)
+    J0 = orc.cufd(0, lam, mu, rho, w.stf, ids, para)["misfit"]
+    ctx = fw.FwiContext(para, 0)
+    for width in (4, 8, 16):
+        for rows in (1, 2):
+            ctx.set_tile_config([width] * 4)
+            ctx.set_tile_rows([rows] * 4)
+            got = ctx.obs(lo, mo, ro, w.stf, ids, write_files=False)
+            for a, b in zip(got, ref):
+                assert rel(a, b) < TOL_DATA, (width, rows)
+            J, gl, gm, gd, gs = ctx.misfit_grad(lam, mu, rho, w.stf, ids)
+            assert abs(J - J0) <= TOL_DATA * abs(J0), (width, rows)
+            for k, a in (("g_lambda", gl), ("g_mu", gm), ("g_den", gd), ("g_stf", gs)):
+                assert rel(a, r1[k]) < TOL_GRAD, (k, width, rows)
+    ctx.close()
+
+
 @pytest.mark.parametrize("case", [
     dict(nz=20, nx=33, nPml=6, nSteps=120, n_shots=1, seed=3),
     dict(nz=37, nx=70, nPml=9, nSteps=160, n_shots=3, seed=4),
