@@ -213,12 +213,13 @@ __device__ __forceinline__ float dd(float p, float q, float s, float t, float r)
   return (C1 * (p - q) - C2 * (s - t)) * r;
 }
 
-// Register budgets (measured on GB300 over the tile widths): forward sweeps
-// 32 registers with one cell per thread (64 warps per SM) and 40 with two;
-// backward sweeps 40 with one cell (48 warps per SM: 8 % faster than 48
-// registers on a 16-shot group, whose sweeps wait on memory latency) and 64
-// with two (32 warps per SM).
-#define FWD_BOUNDS __launch_bounds__(32 * TX, (R == 1 ? 2048 : 1536) / (32 * TX))
+// Register budgets (measured on GB300 over the tile widths; the sweeps wait
+// on memory latency, so resident warps count for more than the few bytes
+// spilled): forward sweeps 32 registers (64 warps per SM; with two cells per
+// thread 9 % faster than 40 registers on a 16-shot group); backward sweeps 40
+// with one cell (48 warps per SM: 8 % faster than 48 registers) and 64 with
+// two (32 warps per SM).
+#define FWD_BOUNDS __launch_bounds__(32 * TX, 2048 / (32 * TX))
 #define BWD_BOUNDS \
   __launch_bounds__(32 * TX, ((R == 1 ? 1536 : 1024) / (32 * TX)) > 0 ? ((R == 1 ? 1536 : 1024) / (32 * TX)) : 1)
 
