@@ -75,19 +75,25 @@ __device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* tm, i
 // initialisation; the caller then loads its own-cell operands (which overlap
 // with the copies) and calls stage_wait.
 template <int NA, int TX, int BOXZ>
-__device__ __forceinline__ void stage_begin(const TileMaps& mp, float* sm, uint64_t* bar, int z0, int x0) {
+__device__ __forceinline__ void stage_issue(const TileMaps& mp, float* sm, uint64_t* bar, int z0, int x0) {
   constexpr int N = BOXZ * (TX + 4);
-  const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
-  if (leader) {
-    mbar_init(bar, 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  if (leader) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
     mbar_expect_tx(bar, NA * N * static_cast<unsigned>(sizeof(float)));
 #pragma unroll
     for (int a = 0; a < NA; ++a) tma_load_2d(sm + a * N, &mp.t[a], z0 - 4, x0 - 2, bar);
   }
+}
+__device__ __forceinline__ void stage_init(uint64_t* bar) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+}
+template <int NA, int TX, int BOXZ>
+__device__ __forceinline__ void stage_begin(const TileMaps& mp, float* sm, uint64_t* bar, int z0, int x0) {
+  stage_init(bar);
+  stage_issue<NA, TX, BOXZ>(mp, sm, bar, z0, x0);
 }
 
 // Waits (bounded) for the staged tiles. On a timeout the error word is raised
@@ -151,10 +157,11 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
 // threadIdx.y the column; `b` is the index of its first cell in a staged box
 // (column stride BOXZ = TZ + 8).
 // Programmatic dependent launch: a sweep lets the next sweep's blocks be
-// scheduled as soon as all of its own blocks have started, and waits for the
-// previous sweep to complete (and its writes to be visible) before it
-// touches any field. The parameter reads and tile classification before the
-// wait overlap the previous sweep's last blocks.
+// scheduled as soon as all of its own blocks have started, and waits
+// (pdl_wait) for the previous sweep to complete, and its writes to be
+// visible, before it touches any field. The parameter reads, the tile
+// classification and, in fast tiles, the loads of the media (which no sweep
+// writes) come before the wait and overlap the previous sweep's last blocks.
 #define SWEEP_KERNEL_TILE(TZ_)                                                 \
   const int shot = K == 1 ? 0 : static_cast<int>(blockIdx.z);                  \
   const Geo& g0 = P.slots[shot].g;                                             \
@@ -165,8 +172,7 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
   const bool fast = static_cast<int>(blockIdx.x) >= ts.ftz0 &&                 \
                     static_cast<int>(blockIdx.x) < ts.ftz1 &&                  \
                     static_cast<int>(blockIdx.y) >= ts.ftx0 &&                 \
-                    static_cast<int>(blockIdx.y) < ts.ftx1;                    \
-  asm volatile("griddepcontrol.wait;" ::: "memory");
+                    static_cast<int>(blockIdx.y) < ts.ftx1;
 
 #define SWEEP_BODY_SLOT()                                                      \
   const ShotSlot& S = P.slots[shot];                                           \
@@ -180,9 +186,31 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
   const bool special = !(z0 + (TZ_) - 1 < sh.rbz0 || z0 > sh.rbz1 ||           \
                          x0 + TX - 1 < sh.rbx0 || x0 > sh.rbx1);
 
-// Stages the tile and sets the thread's first cell (z, x), its global index
-// i and its box index b. A thread whose first cell is outside the grid
-// leaves (with R > 1 its later cells are checked by the edge body).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Fast tiles: the thread's first cell (z, x), its global index i and its box
+// index b (every cell of a fast tile is inside the grid).
+#define SWEEP_CELL(BOXZ_, R_)                                                  \
+  const Fields& f = S.f;                                                       \
+  const MediaD& m = S.m;                                                       \
+  const int z = z0 + (R_) * static_cast<int>(threadIdx.x), x = x0 + threadIdx.y; \
+  const size_t ldz = static_cast<size_t>(g.ldz);                               \
+  const size_t i = static_cast<size_t>(x) * ldz + z;                           \
+  const int b = (threadIdx.y + 2) * (BOXZ_) + (R_) * threadIdx.x + 4;
+
+// Fast tiles: the staging barrier is set up before the media loads and the
+// tile copies are issued right after pdl_wait (SWEEP_TMA).
+#define SWEEP_SMEM(BOXZ_)                                                      \
+  constexpr int N = (BOXZ_) * (TX + 4);                                        \
+  extern __shared__ __align__(128) float sm[];                                 \
+  __shared__ __align__(8) uint64_t bar;                                        \
+  stage_init(&bar);
+#define SWEEP_TMA(NA, BOXZ_) stage_issue<NA, TX, (BOXZ_)>(P.maps[shot], sm, &bar, z0, x0);
+
+// Edge tiles (after pdl_wait): stages the tile and sets the thread's first
+// cell (z, x), its global index i and its box index b. A thread whose first
+// cell is outside the grid leaves (with R > 1 its later cells are checked by
+// the edge body).
 #define SWEEP_STAGE(NA, BOXZ_, R_)                                             \
   constexpr int N = (BOXZ_) * (TX + 4);                                        \
   extern __shared__ __align__(128) float sm[];                                 \
@@ -233,6 +261,7 @@ __device__ __forceinline__ void fwd_stress_edge(const SweepPack<K>& P, int shot,
                                                 unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
+  pdl_wait();
   SWEEP_STAGE(2, BOXZ, R)
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
@@ -308,6 +337,7 @@ template <int TX, int K, int R>
 __device__ __forceinline__ void fwd_velocity_edge(const SweepPack<K>& P, int shot, int z0, int x0, unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
+  pdl_wait();
   SWEEP_STAGE(3, BOXZ, R)
   if (!stage_wait(&bar, err)) return;
   const float* s_szz = sm;
@@ -354,6 +384,7 @@ template <int TX, int K, int R>
 __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
+  pdl_wait();
   SWEEP_STAGE(5, BOXZ, R)
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
@@ -478,6 +509,7 @@ template <int TX, int K, int R>
 __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
+  pdl_wait();
   SWEEP_STAGE(5, BOXZ, R)
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
@@ -612,10 +644,13 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
 template <int TX, int K>
 __device__ __forceinline__ void fwd_stress_fast1(const SweepPack<K>& P, int shot, int z0, int x0, int it, unsigned* err) {
   SWEEP_FAST_SLOT(kTileZ)
-  SWEEP_STAGE(2, kBoxZ, 1)
+  SWEEP_CELL(kBoxZ, 1)
+  SWEEP_SMEM(kBoxZ)
+  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
+  pdl_wait();
+  SWEEP_TMA(2, kBoxZ)
   float szz = f.szz[i], sxx = f.sxx[i];
   const float sxz = f.sxz[i];
-  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
   if (!stage_wait(&bar, err)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
@@ -646,8 +681,12 @@ template <int TX, int K>
 __device__ __forceinline__ void fwd_velocity_fast1(const SweepPack<K>& P, int shot, int z0, int x0, unsigned* err) {
   SWEEP_FAST_SLOT(kTileZ)
   (void)special;
-  SWEEP_STAGE(3, kBoxZ, 1)
-  const float vz = f.vz[i], vx = f.vx[i], bA = m.bycA[i], bB = m.bycB[i];
+  SWEEP_CELL(kBoxZ, 1)
+  SWEEP_SMEM(kBoxZ)
+  const float bA = m.bycA[i], bB = m.bycB[i];
+  pdl_wait();
+  SWEEP_TMA(3, kBoxZ)
+  const float vz = f.vz[i], vx = f.vx[i];
   if (!stage_wait(&bar, err)) return;
   const float* s_szz = sm;
   const float* s_sxx = sm + N;
@@ -673,9 +712,12 @@ __device__ __forceinline__ void fwd_stress_fast2(const SweepPack<K>& P, int shot
   static_assert(R == 2, "the forward fast bodies handle two depths per thread");
   constexpr int TZ = 32 * R, BOXZ = TZ + 8;
   SWEEP_FAST_SLOT(TZ)
-  SWEEP_STAGE(2, BOXZ, R)
-  const float2 szz = ld2(f.szz + i), sxx = ld2(f.sxx + i), sxz = ld2(f.sxz + i);
+  SWEEP_CELL(BOXZ, R)
+  SWEEP_SMEM(BOXZ)
   const float2 lam = ld2(m.lam + i), l2m = ld2(m.l2m + i), amu = ld2(m.aveMu + i);
+  pdl_wait();
+  SWEEP_TMA(2, BOXZ)
+  const float2 szz = ld2(f.szz + i), sxx = ld2(f.sxx + i), sxz = ld2(f.sxz + i);
   if (!stage_wait(&bar, err)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
@@ -723,8 +765,12 @@ __device__ __forceinline__ void fwd_velocity_fast2(const SweepPack<K>& P, int sh
   constexpr int TZ = 32 * R, BOXZ = TZ + 8;
   SWEEP_FAST_SLOT(TZ)
   (void)special;
-  SWEEP_STAGE(3, BOXZ, R)
-  const float2 vz = ld2(f.vz + i), vx = ld2(f.vx + i), bA = ld2(m.bycA + i), bB = ld2(m.bycB + i);
+  SWEEP_CELL(BOXZ, R)
+  SWEEP_SMEM(BOXZ)
+  const float2 bA = ld2(m.bycA + i), bB = ld2(m.bycB + i);
+  pdl_wait();
+  SWEEP_TMA(3, BOXZ)
+  const float2 vz = ld2(f.vz + i), vx = ld2(f.vx + i);
   if (!stage_wait(&bar, err)) return;
   const float* s_szz = sm;
   const float* s_sxx = sm + N;
@@ -782,25 +828,28 @@ template <int TX, int K, int R>
 __device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int TZ = 32 * R, BOXZ = TZ + 8;
   SWEEP_FAST_SLOT(TZ)
-  SWEEP_STAGE(5, BOXZ, R)
+  SWEEP_CELL(BOXZ, R)
+  SWEEP_SMEM(BOXZ)
   const Grads& gr = S.gr;
   const int it = S.nSteps - 2 - j;
   const float dt = g.dt;
   float szz[R], sxx[R], sxz[R], lam[R], l2m[R], amu[R], gl[R], gm[R], w[R], h[R], va_z[R], va_x[R], hx[R];
-  ldr<R>(f.szz + i, szz);
-  ldr<R>(f.sxx + i, sxx);
-  ldr<R>(f.sxz + i, sxz);
   ldr<R>(m.lam + i, lam);
   ldr<R>(m.l2m + i, l2m);
   ldr<R>(m.aveMu + i, amu);
-  ldr<R>(gr.lam + i, gl);
-  ldr<R>(gr.mu + i, gm);
   ldr<R>(m.muw + i, w);
   ldr<R>(m.hs + i, h);
-  ldr<R>(f.vz_a + i, va_z);
-  ldr<R>(f.vx_a + i, va_x);
   ldr<R>(m.hs + i - ldz, hx);
   const float hz0 = m.hs[i - 1], hzx0 = m.hs[i - ldz - 1];
+  pdl_wait();
+  SWEEP_TMA(5, BOXZ)
+  ldr<R>(f.szz + i, szz);
+  ldr<R>(f.sxx + i, sxx);
+  ldr<R>(f.sxz + i, sxz);
+  ldr<R>(gr.lam + i, gl);
+  ldr<R>(gr.mu + i, gm);
+  ldr<R>(f.vz_a + i, va_z);
+  ldr<R>(f.vx_a + i, va_x);
   if (!stage_wait(&bar, err)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
@@ -871,17 +920,20 @@ template <int TX, int K, int R>
 __device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int TZ = 32 * R, BOXZ = TZ + 8;
   SWEEP_FAST_SLOT(TZ)
-  SWEEP_STAGE(5, BOXZ, R)
+  SWEEP_CELL(BOXZ, R)
+  SWEEP_SMEM(BOXZ)
   const Grads& gr = S.gr;
   const int it = S.nSteps - 2 - j;
   const int rev = it >= 1;
   const float dt = g.dt;
   float sa[R], xa[R], za[R], bA[R], bB[R], vz[R], vx[R], gd[R], bBj[R];
+  ldr<R>(m.bycA + i, bA);
+  ldr<R>(m.bycB + i, bB);
+  pdl_wait();
+  SWEEP_TMA(5, BOXZ)
   ldr<R>(f.szz_a + i, sa);
   ldr<R>(f.sxx_a + i, xa);
   ldr<R>(f.sxz_a + i, za);
-  ldr<R>(m.bycA + i, bA);
-  ldr<R>(m.bycB + i, bB);
   float bAj0 = 0.0f;
 #pragma unroll
   for (int r = 0; r < R; ++r) vz[r] = vx[r] = gd[r] = bBj[r] = 0.0f;
@@ -967,25 +1019,28 @@ template <int TX, int K>
 __device__ __forceinline__ void bwd_B_fast2(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int TZ = 64, BOXZ = TZ + 8, R = 2;
   SWEEP_FAST_SLOT(TZ)
-  SWEEP_STAGE(5, BOXZ, R)
+  SWEEP_CELL(BOXZ, R)
+  SWEEP_SMEM(BOXZ)
   const Grads& gr = S.gr;
   const int it = S.nSteps - 2 - j;
   const float dt = g.dt;
   float szz[2], sxx[2], sxz[2], lam[2], l2m[2], amu[2], gl[2], gm[2], w[2], h[2], va_z[2], va_x[2], hx[2];
-  ldr<2>(f.szz + i, szz);
-  ldr<2>(f.sxx + i, sxx);
-  ldr<2>(f.sxz + i, sxz);
   ldr<2>(m.lam + i, lam);
   ldr<2>(m.l2m + i, l2m);
   ldr<2>(m.aveMu + i, amu);
-  ldr<2>(gr.lam + i, gl);
-  ldr<2>(gr.mu + i, gm);
   ldr<2>(m.muw + i, w);
   ldr<2>(m.hs + i, h);
-  ldr<2>(f.vz_a + i, va_z);
-  ldr<2>(f.vx_a + i, va_x);
   ldr<2>(m.hs + i - ldz, hx);
   const float hz0 = m.hs[i - 1], hzx0 = m.hs[i - ldz - 1];
+  pdl_wait();
+  SWEEP_TMA(5, BOXZ)
+  ldr<2>(f.szz + i, szz);
+  ldr<2>(f.sxx + i, sxx);
+  ldr<2>(f.sxz + i, sxz);
+  ldr<2>(gr.lam + i, gl);
+  ldr<2>(gr.mu + i, gm);
+  ldr<2>(f.vz_a + i, va_z);
+  ldr<2>(f.vx_a + i, va_x);
   if (!stage_wait(&bar, err)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
@@ -1071,17 +1126,20 @@ template <int TX, int K>
 __device__ __forceinline__ void bwd_C_fast2(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int TZ = 64, BOXZ = TZ + 8, R = 2;
   SWEEP_FAST_SLOT(TZ)
-  SWEEP_STAGE(5, BOXZ, R)
+  SWEEP_CELL(BOXZ, R)
+  SWEEP_SMEM(BOXZ)
   const Grads& gr = S.gr;
   const int it = S.nSteps - 2 - j;
   const int rev = it >= 1;
   const float dt = g.dt;
   float sa[2], xa[2], za[2], bA[2], bB[2], vz[2], vx[2], gd[2], bBj[2];
+  ldr<2>(m.bycA + i, bA);
+  ldr<2>(m.bycB + i, bB);
+  pdl_wait();
+  SWEEP_TMA(5, BOXZ)
   ldr<2>(f.szz_a + i, sa);
   ldr<2>(f.sxx_a + i, xa);
   ldr<2>(f.sxz_a + i, za);
-  ldr<2>(m.bycA + i, bA);
-  ldr<2>(m.bycB + i, bB);
   float bAj0 = 0.0f;
   vz[0] = vz[1] = vx[0] = vx[1] = gd[0] = gd[1] = bBj[0] = bBj[1] = 0.0f;
   if (rev) {
