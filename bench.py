@@ -221,6 +221,10 @@ def main():
     ap.add_argument("--cpu-sample-steps", type=int, default=3000)
     ap.add_argument("--nsteps", type=int, default=None,
                     help="override the workload's time steps (small cases for profiler captures)")
+    ap.add_argument("--tile-widths", default=None,
+                    help="fix the four sweeps' tile widths, e.g. 4,8,4,4 (default: autotuned)")
+    ap.add_argument("--tile-rows", default=None,
+                    help="fix the four sweeps' depths per thread, e.g. 2,2,1,1 (default: autotuned)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -272,6 +276,10 @@ def main():
     tmp = tempfile.mkdtemp()
     para = w.write_files(tmp)
     ctx = fw.FwiContext(para, local_rank)
+    if args.tile_widths:
+        ctx.set_tile_config([int(v) for v in args.tile_widths.split(",")])
+    if args.tile_rows:
+        ctx.set_tile_rows([int(v) for v in args.tile_rows.split(",")])
     ids = list(range(len(w.shots)))
     obs = ctx.obs(*w.moduli(w.vp_obs), w.stf, ids, write_files=False)
     lam, mu, rho = w.moduli()
