@@ -59,6 +59,8 @@ def workload(name, nsteps=None, shots=None):
 
     if name == "small_layered":
         return synthetic.small_layered(**({"nSteps": nsteps} if nsteps else {}))
+    if name == "faulted_grf":
+        return synthetic.faulted_grf(shot_subset=shots or 16, **({"nSteps": nsteps} if nsteps else {}))
     if name == "batched_uneven":
         kw = {"n_shots": shots or 64}
         if nsteps:  # scale the record lengths down (profiler captures)
@@ -93,8 +95,9 @@ def describe(w):
                 f"windows {min(c for c, _ in sz) // w.nz_pad - 2 * w.nPml}..{max(c for c, _ in sz) // w.nz_pad - 2 * w.nPml}"
                 f" columns, record lengths {min(n for _, n in sz)}..{max(n for _, n in sz)} steps, Ricker 8-12 Hz, "
                 f"dx {w.dx} m, dt {w.dt * 1e3:g} ms, FP32; one misfit+gradient per step")
+    shots = f"{len(w.shots)} of the survey's 128 shots" if w.name == "faulted_grf" else f"{len(w.shots)} shot(s)"
     return (f"{w.name}: {w.nz}x{w.nx} interior + {w.nPml} CPML (nPad {w.nPad}) = {w.nz_pad}x{w.nx_pad} cells, "
-            f"{w.nSteps} steps, {len(w.shots)} shot(s), dx {w.dx} m, dt {w.dt * 1e3:g} ms, FP32; "
+            f"{w.nSteps} steps, {shots}, dx {w.dx} m, dt {w.dt * 1e3:g} ms, FP32; "
             f"one misfit+gradient per step")
 
 
@@ -213,8 +216,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dipping_grf", choices=["dipping_grf", "small_layered", "batched_uneven"])
-    ap.add_argument("--shots", type=int, default=None, help="shots of the batched_uneven workload (default 64)")
+    ap.add_argument("--workload", default="dipping_grf", choices=["dipping_grf", "small_layered", "batched_uneven", "faulted_grf"])
+    ap.add_argument("--shots", type=int, default=None, help="shots of the batched_uneven workload (default 64) / of the faulted_grf survey (default 16 of 128)")
     ap.add_argument("--compare-single", action="store_true",
                     help="also time one step with one shot per launch on the same workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")

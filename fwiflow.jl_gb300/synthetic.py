@@ -125,6 +125,41 @@ def dipping_grf(seed: int = 2, nz: int = 512, nx: int = 1536, nSteps: int = 3000
     return Workload("dipping_grf", nz, nx, nPml, nPad, 10.0, 10.0, 0.001, nSteps, 10.0, vp, vp_obs, shots, stf)
 
 
+def faulted_grf(seed: int = 5, nz: int = 1024, nx: int = 3072, nSteps: int = 6000, n_shots: int = 128,
+                shot_subset: Optional[int] = None) -> Workload:
+    """The full-scale model: 8 layers Vp 1500..4500 m/s cut by 3 normal faults
+    (60 degree fault planes at seeded positions, hanging wall thrown down by
+    10-40 cells), times (1 + 0.03 GRF(corr 20)); dx 5 m, dt 0.5 ms, f0 15 Hz,
+    nPml 40; n_shots sources evenly spread at depth 2, receivers on every
+    column at depth 2. The observed data come from the model, the starting
+    model is the model smoothed by 20 cells. shot_subset keeps the first that
+    many shots of the evenly spread set (a slice of the survey for timing)."""
+    from .gradcheck import smooth
+
+    rng = np.random.default_rng(seed)
+    nPml = 40
+    nPad = default_nPad(nz, nPml)
+    zz, xx = np.meshgrid(np.arange(nz, dtype=np.float64), np.arange(nx, dtype=np.float64), indexing="ij")
+    shift = np.zeros((nz, nx))
+    for _ in range(3):
+        xf = rng.uniform(0.15, 0.85) * nx
+        throw = rng.uniform(10.0, 40.0)
+        # hanging wall: right of the plane x = xf + (z / tan 60)
+        shift += np.where(xx > xf + zz / np.tan(np.deg2rad(60.0)), throw, 0.0)
+    depth = zz - shift
+    k = np.clip(np.floor(depth / (nz / 8)), 0, 7)
+    base = 1500.0 + (4500.0 - 1500.0) * k / 7
+    true = base * (1.0 + 0.03 * gaussian_random_field((nz, nx), 20.0, rng))
+    vp0 = smooth(true, 20.0)
+    xs = np.linspace(16, nx - 17, n_shots).astype(int)
+    if shot_subset is not None:
+        xs = xs[:shot_subset]
+    shots = [{"z_src": 2, "x_src": int(x), "z_rec": [2] * nx, "x_rec": list(range(nx))} for x in xs]
+    stf = np.repeat(sourceGene(15.0, nSteps, 0.0005), len(shots), axis=0)
+    return Workload("faulted_grf", nz, nx, nPml, nPad, 5.0, 5.0, 0.0005, nSteps, 15.0, padding(vp0, nPml, nPad),
+                    padding(true, nPml, nPad), shots, stf)
+
+
 def batched_uneven(seed: int = 3, nz: int = 512, nx: int = 1536, n_shots: int = 64, width=(400, 1536),
                    steps=(1500, 4000), f0=(8.0, 12.0), nSteps: Optional[int] = None) -> Workload:
     """The dipping_grf model family with n_shots shots, each with its own
