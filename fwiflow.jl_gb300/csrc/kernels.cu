@@ -136,8 +136,18 @@ __device__ __forceinline__ int ring_index(const Geo& g, int z, int x) {
   return -1;
 }
 
+// a / K of the CPML formulas, with the division skipped where K == 1 (exact:
+// a / 1 == a), i.e. everywhere outside the CPML.
+__device__ __forceinline__ float kdiv(float a, float K) { return K == 1.0f ? a : a / K; }
+
 __device__ __forceinline__ bool in_box(int z, int x, int z0, int z1, int x0, int x1) {
   return z >= z0 && z <= z1 && x >= x0 && x <= x1;
+}
+
+// Whether the tile of tz depths x tx columns at (z0, x0) meets the bounding
+// box of the shot's receivers and source.
+__device__ __forceinline__ bool tile_meets_shot_box(const ShotD& sh, int z0, int x0, int tz, int tx) {
+  return !(z0 + tz - 1 < sh.rbz0 || z0 > sh.rbz1 || x0 + tx - 1 < sh.rbx0 || x0 > sh.rbx1);
 }
 
 // Receiver list of the 32 x 8 bin holding (z, x).
@@ -207,28 +217,29 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
   stage_init(&bar);
 #define SWEEP_TMA(NA, BOXZ_) stage_issue<NA, TX, (BOXZ_)>(P.maps[shot], sm, &bar, z0, x0);
 
-// Edge tiles (after pdl_wait): stages the tile and sets the thread's first
-// cell (z, x), its global index i and its box index b. A thread whose first
-// cell is outside the grid leaves (with R > 1 its later cells are checked by
-// the edge body).
-#define SWEEP_STAGE(NA, BOXZ_, R_)                                             \
-  constexpr int N = (BOXZ_) * (TX + 4);                                        \
-  extern __shared__ __align__(128) float sm[];                                 \
-  __shared__ __align__(8) uint64_t bar;                                        \
-  stage_begin<NA, TX, (BOXZ_)>(P.maps[shot], sm, &bar, z0, x0);                \
+// Edge tiles: the thread's first cell (z, x), its global index i, its box
+// index b and whether the cell lies in the grid (`live`; a thread with no
+// cell in the grid takes part in the staging set-up only, and the tile's
+// first thread, which issues and awaits the copies, is always live).
+#define SWEEP_EDGE_CELL(BOXZ_, R_)                                             \
   const Fields& f = S.f;                                                       \
   const MediaD& m = S.m;                                                       \
   const CpmlD& c = S.c;                                                        \
   const int z = z0 + (R_) * static_cast<int>(threadIdx.x), x = x0 + threadIdx.y; \
-  if (z >= g.nz || x >= g.nx) return;                                          \
+  const bool live = z < g.nz && x < g.nx;                                      \
+  const int rows_in = live ? g.nz - z : 0;                                     \
   const size_t ldz = static_cast<size_t>(g.ldz);                               \
   const size_t i = static_cast<size_t>(x) * ldz + z;                           \
-  const int b = (threadIdx.y + 2) * (BOXZ_) + (R_) * threadIdx.x + 4;          \
-  (void)N;                                                                     \
-  (void)b;                                                                     \
-  (void)f;                                                                     \
-  (void)m;                                                                     \
-  (void)c;
+  const int b = (threadIdx.y + 2) * (BOXZ_) + (R_) * threadIdx.x + 4;           \
+  (void)rows_in;
+
+// Values of the thread's R depths that lie in the grid (rows_in of them);
+// the others are left 0.
+template <int R>
+__device__ __forceinline__ void ldrows(const float* p, int rows_in, float (&v)[R]) {
+#pragma unroll
+  for (int r = 0; r < R; ++r) v[r] = r < rows_in ? p[r] : 0.0f;
+}
 
 // Paired loads / stores of two adjacent depths (8-byte aligned: even depth,
 // ldz a multiple of 32, even box index).
@@ -261,9 +272,13 @@ __device__ __forceinline__ void fwd_stress_edge(const SweepPack<K>& P, int shot,
                                                 unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
+  SWEEP_EDGE_CELL(BOXZ, R)
+  SWEEP_SMEM(BOXZ)
   pdl_wait();
-  SWEEP_STAGE(2, BOXZ, R)
+  SWEEP_TMA(2, BOXZ)
+  if (!live) return;
   const ShotD& sh = S.sh;
+  const bool rec_tile = tile_meets_shot_box(sh, z0, x0, 32 * R, TX);
   const StoreD& st = S.st;
   if (!stage_wait(&bar, err)) return;
   const float* s_vz = sm;
@@ -320,11 +335,13 @@ __device__ __forceinline__ void fwd_stress_edge(const SweepPack<K>& P, int shot,
     }
     // The velocity sweep that follows does not change the stresses, so the
     // sample of step it+1 is taken here.
-    const int2 rr = bin_range(sh, z, x);
-    for (int k = rr.x; k < rr.y; ++k) {
-      const int r = sh.blk_rec[k];
-      if (sh.rec_z[r] == z && sh.rec_x[r] == x)
-        sh.data[static_cast<size_t>(r) * sh.nSteps + it + 1] = szz + 3.0f * sxx;
+    if (rec_tile) {
+      const int2 rr = bin_range(sh, z, x);
+      for (int k = rr.x; k < rr.y; ++k) {
+        const int r = sh.blk_rec[k];
+        if (sh.rec_z[r] == z && sh.rec_x[r] == x)
+          sh.data[static_cast<size_t>(r) * sh.nSteps + it + 1] = szz + 3.0f * sxx;
+      }
     }
   };
 #pragma unroll
@@ -337,8 +354,11 @@ template <int TX, int K, int R>
 __device__ __forceinline__ void fwd_velocity_edge(const SweepPack<K>& P, int shot, int z0, int x0, unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
+  SWEEP_EDGE_CELL(BOXZ, R)
+  SWEEP_SMEM(BOXZ)
   pdl_wait();
-  SWEEP_STAGE(3, BOXZ, R)
+  SWEEP_TMA(3, BOXZ)
+  if (!live) return;
   if (!stage_wait(&bar, err)) return;
   const float* s_szz = sm;
   const float* s_sxx = sm + N;
@@ -384,11 +404,28 @@ template <int TX, int K, int R>
 __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
+  SWEEP_EDGE_CELL(BOXZ, R)
+  SWEEP_SMEM(BOXZ)
+  const Grads& gr = S.gr;
+  float p_lam[R], p_l2m[R], p_amu[R], p_w[R], p_h[R];
+  float p_szz[R], p_sxx[R], p_sxz[R], p_gl[R], p_gm[R], p_vza[R], p_vxa[R];
+  ldrows<R>(m.lam + i, rows_in, p_lam);
+  ldrows<R>(m.l2m + i, rows_in, p_l2m);
+  ldrows<R>(m.aveMu + i, rows_in, p_amu);
+  ldrows<R>(m.muw + i, rows_in, p_w);
+  ldrows<R>(m.hs + i, rows_in, p_h);
   pdl_wait();
-  SWEEP_STAGE(5, BOXZ, R)
+  SWEEP_TMA(5, BOXZ)
+  ldrows<R>(f.szz + i, rows_in, p_szz);
+  ldrows<R>(f.sxx + i, rows_in, p_sxx);
+  ldrows<R>(f.sxz + i, rows_in, p_sxz);
+  ldrows<R>(gr.lam + i, rows_in, p_gl);
+  ldrows<R>(gr.mu + i, rows_in, p_gm);
+  ldrows<R>(f.vz_a + i, rows_in, p_vza);
+  ldrows<R>(f.vx_a + i, rows_in, p_vxa);
+  if (!live) return;
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
-  const Grads& gr = S.gr;
   const int it = S.nSteps - 2 - j;  // this shot's time step at backward iteration j
   const float dt = g.dt;
   if (!stage_wait(&bar, err)) return;
@@ -397,11 +434,11 @@ __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int 
   const float* s_szz_a = sm + 2 * N;
   const float* s_sxx_a = sm + 3 * N;
   const float* s_sxz_a = sm + 4 * N;
-  auto cell = [&](const int z, const size_t i, const int b) {
-  float szz = f.szz[i], sxx = f.sxx[i], sxz = f.sxz[i];
-  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
-  const float gl = gr.lam[i], gm = gr.mu[i], w = m.muw[i], h = m.hs[i];
-  const float va_z = f.vz_a[i], va_x = f.vx_a[i], bA = m.bycA[i], bB = m.bycB[i];
+  auto cell = [&](const int r, const int z, const size_t i, const int b) {
+  float szz = p_szz[r], sxx = p_sxx[r], sxz = p_sxz[r];
+  const float lam = p_lam[r], l2m = p_l2m[r], amu = p_amu[r];
+  const float gl = p_gl[r], gm = p_gm[r], w = p_w[r], h = p_h[r];
+  const float va_z = p_vza[r], va_x = p_vxa[r];
   const bool interior = in_box(z, x, g.zi0, g.zi1, g.xi0, g.xi1);
   const bool src = (z == sh.src_z && x == sh.src_x);
   const int k = ring_index(g, z, x);
@@ -472,33 +509,39 @@ __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int 
     const float dszz_dx = -sdp(s_szz_a, b, BOXZ, g.rdx);
     const float dsxx_dx = -sdp(s_sxx_a, b, BOXZ, g.rdx);
     const float dsxz_dz = -sdm(s_sxz_a, b, 1, g.rdz);
-    float t = lam * dszz_dx / Kx * dt + l2m * dsxx_dx / Kx * dt + amu / Kzh * dsxz_dz * dt;
+    float t = kdiv(lam * dszz_dx, Kx) * dt + kdiv(l2m * dsxx_dx, Kx) * dt + kdiv(amu, Kzh) * dsxz_dz * dt;
     const float ax = c.a_x[x], azh = c.a_zh[z];
     if (ax != 0.0f) t += ax * (-gdp(f.m_dvx_dx, i, ldz, g.rdx));
     if (azh != 0.0f) t += azh * (-gdm(f.m_dvx_dz, i, 1, g.rdz));
     const float v = va_x + t;
     f.vx_a[i] = v;
-    if (xp) f.m_dsxx_dx[i] = c.b_xh[x] * f.m_dsxx_dx[i] + bB * v * dt;
-    if (zp) f.m_dsxz_dz[i] = c.b_z[z] * f.m_dsxz_dz[i] + bB * v * dt;
+    if (xp || zp) {
+      const float bB = m.bycB[i];
+      if (xp) f.m_dsxx_dx[i] = c.b_xh[x] * f.m_dsxx_dx[i] + bB * v * dt;
+      if (zp) f.m_dsxz_dz[i] = c.b_z[z] * f.m_dsxz_dz[i] + bB * v * dt;
+    }
   }
   {
     const float Kz = c.K_z[z], Kxh = c.K_xh[x];
     const float dszz_dz = -sdp(s_szz_a, b, 1, g.rdz);
     const float dsxx_dz = -sdp(s_sxx_a, b, 1, g.rdz);
     const float dsxz_dx = -sdm(s_sxz_a, b, BOXZ, g.rdx);
-    float t = l2m * dszz_dz / Kz * dt + lam * dsxx_dz / Kz * dt + amu / Kxh * dsxz_dx * dt;
+    float t = kdiv(l2m * dszz_dz, Kz) * dt + kdiv(lam * dsxx_dz, Kz) * dt + kdiv(amu, Kxh) * dsxz_dx * dt;
     const float az = c.a_z[z], axh = c.a_xh[x];
     if (az != 0.0f) t += az * (-gdp(f.m_dvz_dz, i, 1, g.rdz));
     if (axh != 0.0f) t += axh * (-gdm(f.m_dvz_dx, i, ldz, g.rdx));
     const float v = va_z + t;
     f.vz_a[i] = v;
-    if (xp) f.m_dsxz_dx[i] = c.b_x[x] * f.m_dsxz_dx[i] + bA * v * dt;
-    if (zp) f.m_dszz_dz[i] = c.b_zh[z] * f.m_dszz_dz[i] + bA * v * dt;
+    if (xp || zp) {
+      const float bA = m.bycA[i];
+      if (xp) f.m_dsxz_dx[i] = c.b_x[x] * f.m_dsxz_dx[i] + bA * v * dt;
+      if (zp) f.m_dszz_dz[i] = c.b_zh[z] * f.m_dszz_dz[i] + bA * v * dt;
+    }
   }
   };
 #pragma unroll
   for (int r = 0; r < R; ++r)
-    if (z + r < g.nz) cell(z + r, i + r, b + r);
+    if (z + r < g.nz) cell(r, z + r, i + r, b + r);
 }
 
 // C: res_injection (utilities.cu:569-580) + el_stress_adj (el_stress_adj.cu:53-97)
@@ -509,16 +552,32 @@ template <int TX, int K, int R>
 __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
+  SWEEP_EDGE_CELL(BOXZ, R)
+  SWEEP_SMEM(BOXZ)
+  const Grads& gr = S.gr;
+  const int rev = S.nSteps - 2 - j >= 1;
+  float p_bA[R], p_bB[R], p_amu[R], p_lam[R], p_l2m[R], p_sa[R], p_xa[R], p_za[R], p_vz[R], p_vx[R], p_gd[R];
+  ldrows<R>(m.bycA + i, rows_in, p_bA);
+  ldrows<R>(m.bycB + i, rows_in, p_bB);
+  ldrows<R>(m.aveMu + i, rows_in, p_amu);
+  ldrows<R>(m.lam + i, rows_in, p_lam);
+  ldrows<R>(m.l2m + i, rows_in, p_l2m);
   pdl_wait();
-  SWEEP_STAGE(5, BOXZ, R)
+  SWEEP_TMA(5, BOXZ)
+  ldrows<R>(f.szz_a + i, rows_in, p_sa);
+  ldrows<R>(f.sxx_a + i, rows_in, p_xa);
+  ldrows<R>(f.sxz_a + i, rows_in, p_za);
+  ldrows<R>(f.vz + i, rev ? rows_in : 0, p_vz);
+  ldrows<R>(f.vx + i, rev ? rows_in : 0, p_vx);
+  ldrows<R>(gr.den + i, rev ? rows_in : 0, p_gd);
+  if (!live) return;
   const ShotD& sh = S.sh;
   const StoreD& st = S.st;
-  const Grads& gr = S.gr;
+  const bool rec_tile = tile_meets_shot_box(sh, z0, x0, 32 * R, TX);
   // Backward iteration j handles res_injection + el_stress_adj of step
   // it = nSteps - 2 - j (j = -1: the shot's last step) and the reverse
   // velocity of step it - 1.
   const int it = S.nSteps - 2 - j;
-  const int rev = it >= 1;
   const float dt = g.dt;
   if (!stage_wait(&bar, err)) return;
   const float* s_vz_a = sm;
@@ -526,32 +585,29 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
   const float* s_szz = sm + 2 * N;
   const float* s_sxx = sm + 3 * N;
   const float* s_sxz = sm + 4 * N;
-  auto cell = [&](const int z, const size_t i, const int b) {
-  float sa = f.szz_a[i], xa = f.sxx_a[i], za = f.sxz_a[i];
-  const float bA = m.bycA[i], bB = m.bycB[i], amu = m.aveMu[i], lam = m.lam[i], l2m = m.l2m[i];
-  float vz = 0.0f, vx = 0.0f, gd = 0.0f;
-  if (rev) {
-    vz = f.vz[i];
-    vx = f.vx[i];
-    gd = gr.den[i];
-  }
+  auto cell = [&](const int r, const int z, const size_t i, const int b) {
+  float sa = p_sa[r], xa = p_xa[r], za = p_za[r];
+  const float bA = p_bA[r], bB = p_bB[r], amu = p_amu[r], lam = p_lam[r], l2m = p_l2m[r];
+  float vz = p_vz[r], vx = p_vx[r], gd = p_gd[r];
   const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
   bool injected = false;
-  const int2 rr = bin_range(sh, z, x);
-  for (int k = rr.x; k < rr.y; ++k) {
-    const int r = sh.blk_rec[k];
-    if (sh.rec_z[r] == z && sh.rec_x[r] == x) {
-      const float rv = sh.res[static_cast<size_t>(r) * sh.nSteps + it];
-      sa += rv;
-      xa += 3.0f * rv;
-      injected = true;
+  if (rec_tile) {
+    const int2 rr = bin_range(sh, z, x);
+    for (int k = rr.x; k < rr.y; ++k) {
+      const int r = sh.blk_rec[k];
+      if (sh.rec_z[r] == z && sh.rec_x[r] == x) {
+        const float rv = sh.res[static_cast<size_t>(r) * sh.nSteps + it];
+        sa += rv;
+        xa += 3.0f * rv;
+        injected = true;
+      }
     }
   }
   if (dom) {
     {
       const float dvz_dx = -sdp(s_vz_a, b, BOXZ, g.rdx);
       const float dvx_dz = -sdp(s_vx_a, b, 1, g.rdz);
-      float t = dvz_dx / c.K_x[x] * bA * dt + dvx_dz / c.K_z[z] * bB * dt;
+      float t = kdiv(dvz_dx, c.K_x[x]) * bA * dt + kdiv(dvx_dz, c.K_z[z]) * bB * dt;
       const float ax = c.a_x[x], az = c.a_z[z];
       if (ax != 0.0f) t += ax * (-gdp(f.m_dsxz_dx, i, ldz, g.rdx));
       if (az != 0.0f) t += az * (-gdp(f.m_dsxz_dz, i, 1, g.rdz));
@@ -565,8 +621,8 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
     {
       const float dvx_dx = -sdm(s_vx_a, b, BOXZ, g.rdx);
       const float dvz_dz = -sdm(s_vz_a, b, 1, g.rdz);
-      float tx = bB * dvx_dx / c.K_xh[x] * dt;
-      float tz = bA * dvz_dz / c.K_zh[z] * dt;
+      float tx = kdiv(bB * dvx_dx, c.K_xh[x]) * dt;
+      float tz = kdiv(bA * dvz_dz, c.K_zh[z]) * dt;
       const float axh = c.a_xh[x], azh = c.a_zh[z];
       if (axh != 0.0f) tx += axh * (-gdm(f.m_dsxx_dx, i, ldz, g.rdx));
       if (azh != 0.0f) tz += azh * (-gdm(f.m_dszz_dz, i, 1, g.rdz));
@@ -627,7 +683,7 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
   };
 #pragma unroll
   for (int r = 0; r < R; ++r)
-    if (z + r < g.nz) cell(z + r, i + r, b + r);
+    if (z + r < g.nz) cell(r, z + r, i + r, b + r);
 }
 
 // ---------------------------------------------------------------------------
