@@ -14,7 +14,10 @@ explicit so the preconditioner can enter):
   `descent`  preconditioned steepest descent with a three-point line search;
              a preconditioned step that does not lower the misfit falls back
              to the plain gradient step (which thereby judges it).
-  `lbfgs`    limited-memory BFGS on the plain gradient (two-loop recursion).
+  `lbfgs`    limited-memory BFGS (two-loop recursion) on the plain gradient,
+             or preconditioned: the initial inverse Hessian of each
+             iteration is the scaled diagonal gain of a preconditioner
+             (pseudo-Hessian or learned) at the current model.
 Each records, per iteration, the misfit, the relative model error
 |Vp - Vp_true| / |Vp_true| over the mask and the wall time (GPU work
 synchronised), so `time_to_error` can read the time to a target error.
@@ -198,10 +201,14 @@ def descent(problem: VpProblem, iters: int, precondition: Optional[Callable] = N
 
 
 def lbfgs(problem: VpProblem, iters: int, memory: int = 5, step_max: float = 60.0,
-          target_error: Optional[float] = None) -> History:
-    """L-BFGS (two-loop recursion, memory pairs) on the plain gradient, with
-    the same line search; the first step (and any step after a failed search)
-    is a steepest-descent step."""
+          target_error: Optional[float] = None, gain: Optional[Callable] = None) -> History:
+    """L-BFGS (two-loop recursion, memory pairs) with the same line search;
+    the first step (and any step after a failed search) is a steepest-descent
+    step. gain(vp, g_vp, grads, illum, mask) -> diagonal gain G (None: the
+    plain method) makes it preconditioned: the initial inverse Hessian of each
+    iteration is gamma G at the current model, gamma = s.y / y.(G y) from the
+    newest pair (the steepest-descent steps use G g); the illumination is then
+    accumulated during the gradient runs."""
     h = History()
     vp = problem.vp0.copy()
     t0 = time.perf_counter()
@@ -211,7 +218,13 @@ def lbfgs(problem: VpProblem, iters: int, memory: int = 5, step_max: float = 60.
     h.fallback.append(False)
     S, Y = [], []
     step = step_max
-    J, g, _, _ = problem.misfit_grad(vp)
+    want_illum = gain is not None
+
+    def diag(v, g_, grads, illum):
+        return np.ones_like(g_) if gain is None else gain(problem.full(v), g_, grads, illum, problem.mask)
+
+    J, g, grads, illum = problem.misfit_grad(vp, illumination=want_illum)
+    G = diag(vp, g, grads, illum)
     h.misfit.append(J)
     for _ in range(iters):
         q = g.copy()
@@ -221,7 +234,9 @@ def lbfgs(problem: VpProblem, iters: int, memory: int = 5, step_max: float = 60.
             alphas.append(a)
             q -= a * y
         if S:
-            q *= np.sum(S[-1] * Y[-1]) / np.sum(Y[-1] * Y[-1])
+            q = G * q * (np.sum(S[-1] * Y[-1]) / np.sum(Y[-1] * G * Y[-1]))
+        else:
+            q = G * q
         for (s, y), a in zip(zip(S, Y), reversed(alphas)):
             b = np.sum(y * q) / np.sum(y * s)
             q += (a - b) * s
@@ -238,7 +253,8 @@ def lbfgs(problem: VpProblem, iters: int, memory: int = 5, step_max: float = 60.
         vp_new, _, change = res
         step = min(step_max, 1.5 * change)
         vp_new = np.clip(vp_new, problem.vmin, problem.vmax)
-        J_new, g_new, _, _ = problem.misfit_grad(vp_new)
+        J_new, g_new, grads, illum = problem.misfit_grad(vp_new, illumination=want_illum)
+        G = diag(vp_new, g_new, grads, illum)
         s, y = vp_new - vp, g_new - g
         if np.sum(s * y) > 1e-12 * np.linalg.norm(s) * np.linalg.norm(y):
             S.append(s)
@@ -267,6 +283,30 @@ def pseudo_hessian_preconditioner(eps: Optional[float] = None) -> Callable:
         return g_vp * illumination_gain(illum, mask, EPS if eps is None else eps)
 
     return apply
+
+
+def pseudo_hessian_gain(eps: Optional[float] = None) -> Callable:
+    """The diagonal pseudo-Hessian preconditioner as a gain on the Vp
+    gradient (for L-BFGS's initial inverse Hessian)."""
+    from .precond import EPS, illumination_gain
+
+    def gain(vp, g_vp, grads, illum, mask):
+        return illumination_gain(illum, mask, EPS if eps is None else eps)
+
+    return gain
+
+
+def learned_gain(net) -> Callable:
+    """The network's predicted gain on the Vp gradient: exp of the mean of its
+    three log-gain channels."""
+
+    def gain(vp, g_vp, grads, illum, mask):
+        from .precond import features
+
+        out = net.predict(features(*grads, illum, mask))
+        return np.exp(np.clip(out.mean(axis=0), -30.0, 5.0))
+
+    return gain
 
 
 def learned_preconditioner(net) -> Callable:

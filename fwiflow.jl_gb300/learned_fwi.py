@@ -10,8 +10,10 @@ error, learned vs plain, on one GPU.
 3. Held-out models (seeds eval_seed..): inversions from the starting model
    with plain steepest descent, learned-preconditioned descent (falling back
    to the plain step when its step does not lower the misfit), the exact
-   pseudo-Hessian descent, and plain L-BFGS; each records misfit, model error
-   and wall time per iteration.
+   pseudo-Hessian descent, plain L-BFGS and L-BFGS whose initial inverse
+   Hessian is the learned (lbfgs_learned) or the pseudo-Hessian
+   (lbfgs_pseudo_hessian) gain; each records misfit, model error and wall
+   time per iteration.
 
     python fwiflow.jl_gb300/learned_fwi.py [--train-models 64] [--eval-models 4] [--iters 20] [--out FILE]
 
@@ -109,6 +111,10 @@ def main(argv=None) -> None:
                 h = inversion.descent(prob, args.iters, inversion.pseudo_hessian_preconditioner())
             elif m == "lbfgs":
                 h = inversion.lbfgs(prob, args.iters)
+            elif m == "lbfgs_learned":
+                h = inversion.lbfgs(prob, args.iters, gain=inversion.learned_gain(net))
+            elif m == "lbfgs_pseudo_hessian":
+                h = inversion.lbfgs(prob, args.iters, gain=inversion.pseudo_hessian_gain())
             else:
                 raise ValueError(m)
             d = h.as_dict()
