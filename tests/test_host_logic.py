@@ -121,3 +121,21 @@ def test_no_cpu_fallback_when_library_missing(fw, tmp_path, monkeypatch):
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         _lib.load(str(tmp_path / "missing.so"))
+
+
+def test_benchmark_workloads_are_stable(fw):
+    """The synthetic workloads the benchmark times satisfy the CFL bound of
+    the scheme (max Vp dt / dx * sqrt(2) (9/8 + 1/24) < 1) and have the sizes
+    their descriptions state."""
+    import numpy as np
+
+    from fwiflow_gb300 import synthetic
+
+    courant = np.sqrt(2.0) * (9.0 / 8.0 + 1.0 / 24.0)
+    for w, shape in ((synthetic.dipping_grf(nSteps=10), (608, 1600)),
+                     (synthetic.batched_uneven(n_shots=4, steps=(5, 10)), (608, 1600)),
+                     (synthetic.faulted_grf(nSteps=10, shot_subset=2), (1120, 3152))):
+        assert (w.nz_pad, w.nx_pad) == shape
+        assert max(w.vp.max(), w.vp_obs.max()) * w.dt / w.dx * courant < 1.0
+    f = synthetic.faulted_grf(nSteps=10, n_shots=128, shot_subset=None)
+    assert len(f.shots) == 128 and all(len(s["x_rec"]) == 3072 for s in f.shots[:2])
