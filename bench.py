@@ -443,7 +443,7 @@ def main():
     }
     if single:
         line["one_shot_per_launch"] = single
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and world == 1:  # the host-core baseline is taken at N = 1 only
         g, t, threads = run_cpu_oracle(cpu_oracle_case(w, min(args.cpu_sample_steps, w.nSteps)))
         line["cpu_baseline"] = {"value": g, "unit": unit, "cores": threads, "kind": "port",
                                 "sample": f"first {min(args.cpu_sample_steps, w.nSteps)} of {w.nSteps} time steps, "
