@@ -3,7 +3,8 @@ throughput (Gpts/s = grid cells x time steps x shots per second of one
 misfit + gradient evaluation) against the HBM roofline.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload dipping_grf|small_layered|batched_uneven] [--shots S]
+                    [--workload dipping_grf|small_layered|batched_uneven|faulted_grf] [--shots S]
+                    [--nsteps T] [--tile-widths a,b,c,d] [--tile-rows a,b,c,d]
                     [--compare-single] [--no-cpu-baseline]
 
 One step = one misfit + gradient call (forward sweep with boundary saving,
@@ -13,7 +14,9 @@ library's stream around fwigb_run. `e2e`: the public C-ABI call
 fwigb_misfit_grad_obs with pinned host buffers (model in, gradients out).
 `--impl reference` times the reference algorithm's CPU implementation (the
 oracle restatement, all host threads) on a bounded number of time steps of
-the same workload. With N > 1 (torchrun) every rank runs its own replica.
+the same workload. `cpu_baseline` (N = 1 only): the same oracle on the
+first steps of the same workload. With N > 1 (torchrun) every rank runs
+its own replica.
 Shots with their own aperture window and record length count their own
 cells and steps. `--compare-single` also times one step with one shot per
 launch (groups of one) on the same workload.
