@@ -139,3 +139,22 @@ def test_benchmark_workloads_are_stable(fw):
         assert max(w.vp.max(), w.vp_obs.max()) * w.dt / w.dx * courant < 1.0
     f = synthetic.faulted_grf(nSteps=10, n_shots=128, shot_subset=None)
     assert len(f.shots) == 128 and all(len(s["x_rec"]) == 3072 for s in f.shots[:2])
+
+
+def test_reference_arm_prints_the_contract_line(fw):
+    """bench.py --impl reference (the oracle on the host cores) prints one JSON
+    line with the reference arm's keys, on a small workload."""
+    import subprocess
+    import sys
+
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload",
+                          "small_layered", "--steps", "1", "--warmup", "0", "--cpu-sample-steps", "60"],
+                         capture_output=True, text=True, timeout=300, check=True).stdout
+    line = json.loads(out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "Gpts/s" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": "Gpts/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    for k in ("metric", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling", "vs_baseline",
+              "dtype", "data", "config"):
+        assert k in line, k
