@@ -170,8 +170,9 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
 // scheduled as soon as all of its own blocks have started, and waits
 // (pdl_wait) for the previous sweep to complete, and its writes to be
 // visible, before it touches any field. The parameter reads, the tile
-// classification and, in fast tiles, the loads of the media (which no sweep
-// writes) come before the wait and overlap the previous sweep's last blocks.
+// classification, the staging-barrier set-up and, in fast tiles and backward
+// edge tiles, the loads of the media (which no sweep writes) come before the
+// wait and overlap the previous sweep's last blocks.
 #define SWEEP_KERNEL_TILE(TZ_)                                                 \
   const int shot = K == 1 ? 0 : static_cast<int>(blockIdx.z);                  \
   const Geo& g0 = P.slots[shot].g;                                             \
