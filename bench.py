@@ -3,23 +3,29 @@ throughput (Gpts/s = grid cells x time steps x shots per second of one
 misfit + gradient evaluation) against the HBM roofline.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload dipping_grf|small_layered|batched_uneven|faulted_grf] [--shots S]
-                    [--nsteps T] [--tile-widths a,b,c,d] [--tile-rows a,b,c,d]
-                    [--compare-single] [--no-cpu-baseline]
+                    [--workload batched_uneven|dipping_grf|small_layered|faulted_grf] [--shots S]
+                    [--nsteps T] [--tile-widths a,b,c,d] [--tile-rows a,b,c,d] [--e2e-steps E]
+                    [--no-compare-single] [--no-cpu-baseline] [--cpu-sample-steps T]
 
+Default workload: 64 shots of the 512x1536-interior dipping-layer model, each
+with its own aperture window (400-1536 columns), record length (1500-4000
+steps) and Ricker frequency (8-12 Hz), all in one misfit + gradient call.
 One step = one misfit + gradient call (forward sweep with boundary saving,
 residual, reverse / adjoint sweeps with imaging) over the workload's shots.
 `value`: model, shots and observed data resident in HBM, CUDA events on the
 library's stream around fwigb_run. `e2e`: the public C-ABI call
-fwigb_misfit_grad_obs with pinned host buffers (model in, gradients out).
+fwigb_misfit_grad_obs with pinned host buffers (model in, gradients out),
+min(K, E) calls. `roofline`: per-sweep times of one call measured inside the
+call (an event pair around each sweep step, all shot packs of the step).
+`one_shot_per_launch`: the same call with every shot in a group of its own
+(unless --no-compare-single).
 `--impl reference` times the reference algorithm's CPU implementation (the
 oracle restatement, all host threads) on a bounded number of time steps of
 the same workload. `cpu_baseline` (N = 1 only): the same oracle on the
 first steps of the same workload. With N > 1 (torchrun) every rank runs
 its own replica.
 Shots with their own aperture window and record length count their own
-cells and steps. `--compare-single` also times one step with one shot per
-launch (groups of one) on the same workload.
+cells and steps.
 """
 from __future__ import annotations
 
@@ -219,10 +225,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dipping_grf", choices=["dipping_grf", "small_layered", "batched_uneven", "faulted_grf"])
+    ap.add_argument("--workload", default="batched_uneven",
+                    choices=["batched_uneven", "dipping_grf", "small_layered", "faulted_grf"])
     ap.add_argument("--shots", type=int, default=None, help="shots of the batched_uneven workload (default 64) / of the faulted_grf survey (default 16 of 128)")
-    ap.add_argument("--compare-single", action="store_true",
-                    help="also time one step with one shot per launch on the same workload")
+    ap.add_argument("--no-compare-single", action="store_true",
+                    help="skip the timing of one step with one shot per launch on the same workload")
+    ap.add_argument("--e2e-steps", type=int, default=3, help="end-to-end calls timed (at most --steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-steps", type=int, default=3000)
     ap.add_argument("--nsteps", type=int, default=None,
@@ -335,34 +343,39 @@ def main():
     pts_step = cell_steps
     value = world * pts_step * args.steps / dev_s / 1e9
 
-    # Per-kernel timing for the roofline. Launch counts come from one step
-    # with per-launch events; the duration of a launch from a CUDA graph of
-    # back-to-back launches of that sweep over the whole group (events around
-    # the graph only: per-launch event pairs add ~4 us to every launch).
+    # Per-sweep timing for the roofline, measured inside one call: an event
+    # pair around every sweep step (all shot packs of the step; the pair costs
+    # a few microseconds per step and stops the next sweep's launch from
+    # overlapping this one's tail). A sweep's algorithmic bytes over the call
+    # are its bytes per cell times the cell-steps its launches processed.
     ctx.set_kernel_timing(True)
     ctx.run(1)
-    tot_eager, cnt = ctx.kernel_times()
+    tot_ms, cnt = ctx.kernel_times()
     ctx.set_kernel_timing(False)
     ctx.run(1)
-    us = np.array([ctx.sweep_time(k, 50) for k in range(4)])
-    group_cells = sum(c for c, _ in shot_sizes(w))  # all shots form one group here
-    tot = us * cnt / 1e3  # ms per call by kind
-    k_dom = int(np.argmax(tot))
+    # Supplementary: a CUDA graph of 50 back-to-back sweep steps over the
+    # whole group (no event pair between them).
+    us_graph = np.array([ctx.sweep_time(k, 50) for k in range(4)])
+    cs = sweep_cell_steps(w)
+    k_dom = int(np.argmax(tot_ms))
     peak, peak_kind = peaks()
-    kbytes_launch = [SWEEP_BYTES[k] * group_cells for k in range(4)]
-    achieved = kbytes_launch[k_dom] / (us[k_dom] * 1e-6) / 1e9
-    per_kernel = {SWEEP_NAMES[k]: {"launches": int(cnt[k]), "avg_us": float(us[k]),
-                                   "eager_avg_us": 1e3 * tot_eager[k] / max(cnt[k], 1),
-                                   "share": float(tot[k] / tot.sum()),
-                                   "algorithmic_GBps": kbytes_launch[k] / (us[k] * 1e-6) / 1e9}
+    kbytes_call = [SWEEP_BYTES[k] * cs[k] for k in range(4)]
+    achieved = kbytes_call[k_dom] / (tot_ms[k_dom] * 1e-3) / 1e9
+    per_kernel = {SWEEP_NAMES[k]: {"launches": int(cnt[k]), "avg_us": 1e3 * tot_ms[k] / max(cnt[k], 1),
+                                   "share": float(tot_ms[k] / tot_ms.sum()),
+                                   "algorithmic_GBps": kbytes_call[k] / (tot_ms[k] * 1e-3) / 1e9,
+                                   "graph_avg_us_all_shots": float(us_graph[k])}
                   for k in range(4)}
+    bytes_launch = kbytes_call[k_dom] / max(cnt[k_dom], 1)  # per sweep step, averaged over the call
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "dram_traffic.txt")
     if os.path.exists(tfile):
+        # "<kernel> <DRAM bytes of one sweep step> <cells it covered>"; scaled
+        # to this call's average active cells per sweep step.
         for line in open(tfile):
             parts = line.split()
             if len(parts) >= 3 and parts[0] == SWEEP_KERNELS[k_dom] and not line.startswith("#"):
-                traffic = float(parts[1]) * group_cells / float(parts[2])
+                traffic = float(parts[1]) * (cs[k_dom] / max(cnt[k_dom], 1)) / float(parts[2])
     step_gbps = FWD_ADJ_BYTES * pts_step / (dev_s / args.steps) / 1e9
 
     # End to end through the public C ABI with pinned host buffers.
@@ -392,9 +405,10 @@ def main():
                                              _lib.dptr(out["gm"]), _lib.dptr(out["gd"]), _lib.dptr(gs_h)), ctx._h)
 
     e2e_call()
+    n_e2e = max(1, min(args.steps, args.e2e_steps))
     barrier()
     t1 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(n_e2e):
         e2e_call()
     barrier()
     e2e_s = time.perf_counter() - t1
@@ -402,12 +416,12 @@ def main():
         t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t[0])
-    e2e_val = world * pts_step * args.steps / e2e_s / 1e9
+    e2e_val = world * pts_step * n_e2e / e2e_s / 1e9
     h2d = 3 * w.cells * 8 + stf_h.nbytes + obs_h.nbytes
     d2h = 3 * w.cells * 8 + len(ids) * w.nSteps * 8 + 8
 
     single = None
-    if args.compare_single:
+    if not args.no_compare_single:
         # The same call with one shot per launch (groups of one shot).
         ctx.set_model(lam, mu, rho)
         ctx.stage_shots(w.stf, ids, obs=obs)
@@ -425,7 +439,8 @@ def main():
         s_single = e0.elapsed_time(e1) / 1e3
         ctx.set_batching(max_shots=0)
         single = {"value": pts_step / s_single / 1e9, "unit": unit, "ms_per_step": 1e3 * s_single,
-                  "groups": ctx.last_group_count(), "note": "same call, one shot per launch"}
+                  "groups": ctx.last_group_count(), "batched_over_single": value / (pts_step / s_single / 1e9),
+                  "note": "same call, every shot in a group of its own (one shot per launch)"}
 
     if rank != 0:
         return
@@ -437,10 +452,13 @@ def main():
         "roofline": {"bound": "hbm", "kernel": SWEEP_KERNELS[k_dom], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback 6.8 TB/s",
-                     "traffic": traffic, "algorithmic_bytes_per_launch": kbytes_launch[k_dom],
-                     "launch_timing": "CUDA graph of 50 back-to-back launches, all shots of the group",
-                     "step_algorithmic_GBps": step_gbps, "step_frac": step_gbps / peak, "kernels": per_kernel},
-        "e2e": {"value": e2e_val, "unit": unit, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                     "traffic": traffic, "algorithmic_bytes_per_launch": bytes_launch,
+                     "launch_unit": "one sweep step: the launches of all shot packs of the group at one time step",
+                     "launch_timing": "CUDA events around every sweep step of one misfit + gradient call",
+                     "step_algorithmic_GBps": step_gbps, "step_frac": step_gbps / peak,
+                     "sweeps_ms_per_call": float(tot_ms.sum()), "kernels": per_kernel},
+        "e2e": {"value": e2e_val, "unit": unit, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "calls_timed": n_e2e},
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": clk,
     }

@@ -480,6 +480,10 @@ struct fwigb_ctx {
   int rows[4] = {2, 2, 1, 1};  // depths per thread per sweep (1 or 2)
   bool tuned_fwd = false, tuned_bwd = false;
   bool autotune = true;
+  // Timeout test hook: the first forward sweep of every run lets its bounded
+  // wait run out (after its tiles have landed), so the run ends in
+  // FWIGB_ERR_TIMEOUT.
+  bool inject_timeout = false;
   // per-kernel event timing
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -985,14 +989,15 @@ int plan_groups(fwigb_ctx* ctx, bool adj, std::vector<std::vector<int>>& groups)
 // Launches sweep `w` (0 F1, 1 F2, 2 B, 3 C) with `rows` depths per thread
 // (forward sweeps: 1 or 2) over the first `a` members of the current group at
 // tile width tx, one launch per parameter pack; `arg` is the step (F1) or the
-// backward iteration (B, C). Returns the number of launches.
-int launch_sweep(fwigb_ctx* ctx, int w, int tx, int rows, int a, int arg, bool save, unsigned* d_err) {
+// backward iteration (B, C); `flags` those of launch_fwd_stress (F1 only).
+// Returns the number of launches.
+int launch_sweep(fwigb_ctx* ctx, int w, int tx, int rows, int a, int arg, int flags, unsigned* d_err) {
   cudaStream_t s = ctx->stream;
   const int variant = rows == 2 ? w + 4 : w;
   const size_t base = static_cast<size_t>(variant * 3 + tx_slot(tx));
   auto go = [&](const auto& pk, int n, const SweepGrid& gr) {
     switch (w) {
-      case 0: return launch_fwd_stress(s, tx, rows, pk, n, gr, arg, save, d_err);
+      case 0: return launch_fwd_stress(s, tx, rows, pk, n, gr, arg, flags, d_err);
       case 1: return launch_fwd_velocity(s, tx, rows, pk, n, gr, d_err);
       case 2: return launch_bwd_B(s, tx, rows, pk, n, gr, arg, d_err);
       default: return launch_bwd_C(s, tx, rows, pk, n, gr, arg, d_err);
@@ -1132,14 +1137,14 @@ int autotune(fwigb_ctx* ctx, int nshots, int nx_max, bool adj) {
     for (int q = 0; q < ncand; ++q) {  // warm-up
       int tx, rows;
       cand(q, tx, rows);
-      launch_sweep(ctx, kind, tx, rows, nshots, 0, false, d_err);
+      launch_sweep(ctx, kind, tx, rows, nshots, 0, 0, d_err);
     }
     for (int r = 0; r < kRounds; ++r)
       for (int q = 0; q < ncand; ++q) {
         int tx, rows;
         cand(q, tx, rows);
         CK(cudaEventRecord(ev[2 * (r * kMaxCand + q)], s));
-        for (int k = 0; k < kReps; ++k) launch_sweep(ctx, kind, tx, rows, nshots, 0, false, d_err);
+        for (int k = 0; k < kReps; ++k) launch_sweep(ctx, kind, tx, rows, nshots, 0, 0, d_err);
         CK(cudaEventRecord(ev[2 * (r * kMaxCand + q) + 1], s));
       }
     CK(cudaStreamSynchronize(s));
@@ -1306,8 +1311,9 @@ int run(fwigb_ctx* ctx, int calc_id) {
       const int ntop = nst[0];
       for (int it = 0; it <= ntop - 2; ++it) {
         const int a = active(it);
-        TIMED(0, group_launches += launch_sweep(ctx, 0, ctx->tx[0], ctx->rows[0], a, it, adj, d_err));
-        TIMED(1, group_launches += launch_sweep(ctx, 1, ctx->tx[1], ctx->rows[1], a, 0, false, d_err));
+        const int f1_flags = (adj ? 1 : 0) | (ctx->inject_timeout && it == 0 ? 2 : 0);
+        TIMED(0, group_launches += launch_sweep(ctx, 0, ctx->tx[0], ctx->rows[0], a, it, f1_flags, d_err));
+        TIMED(1, group_launches += launch_sweep(ctx, 1, ctx->tx[1], ctx->rows[1], a, 0, 0, d_err));
       }
       if (if_res) {
         for (int k = 0; k < G; ++k) {
@@ -1394,11 +1400,11 @@ int run(fwigb_ctx* ctx, int calc_id) {
         // then res_injection(nSteps-1) + el_stress_adj, source_grad(nSteps-2),
         // reverse velocity of step nSteps-2 ... (libCUFD.cu:353-445), with
         // backward iteration j meaning step nSteps_k - 2 - j of member k.
-        TIMED(3, group_launches += launch_sweep(ctx, 3, ctx->tx[3], ctx->rows[3], G, -1, false, d_err));
+        TIMED(3, group_launches += launch_sweep(ctx, 3, ctx->tx[3], ctx->rows[3], G, -1, 0, d_err));
         for (int j = 0; j <= ntop - 2; ++j) {
           const int a = active(j);
-          TIMED(2, group_launches += launch_sweep(ctx, 2, ctx->tx[2], ctx->rows[2], a, j, false, d_err));
-          TIMED(3, group_launches += launch_sweep(ctx, 3, ctx->tx[3], ctx->rows[3], a, j, false, d_err));
+          TIMED(2, group_launches += launch_sweep(ctx, 2, ctx->tx[2], ctx->rows[2], a, j, 0, d_err));
+          TIMED(3, group_launches += launch_sweep(ctx, 3, ctx->tx[3], ctx->rows[3], a, j, 0, d_err));
         }
       }
       if (adj || ctx->illum) {
@@ -1416,7 +1422,8 @@ int run(fwigb_ctx* ctx, int calc_id) {
       // launches depend on: the parameter packs (pointers, geometry, TMA
       // maps), tile choices, flags and the buffers of the memsets / residual.
       std::vector<uint64_t> key = {static_cast<uint64_t>(calc_id), static_cast<uint64_t>(ctx->illum),
-                                   static_cast<uint64_t>(ctx->per_trace_taper)};
+                                   static_cast<uint64_t>(ctx->per_trace_taper),
+                                   static_cast<uint64_t>(ctx->inject_timeout)};
       for (int k = 0; k < 4; ++k) key.push_back((static_cast<uint64_t>(ctx->tx[k]) << 8) | ctx->rows[k]);
       const ShotPlan& pl0 = ctx->plans[mem[0]];
       for (uint64_t v : {static_cast<uint64_t>(pl0.nrec), static_cast<uint64_t>(pl0.nSteps),
@@ -1720,7 +1727,7 @@ int fwigb_sweep_time(fwigb_ctx* ctx, int kind, int reps, double* us_per_launch) 
   const int rows = ctx->rows[kind];
   CK(cudaStreamSynchronize(s));
   CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  for (int r = 0; r < reps; ++r) launch_sweep(ctx, kind, ctx->tx[kind], rows, ctx->group_size, 0, false, d_err);
+  for (int r = 0; r < reps; ++r) launch_sweep(ctx, kind, ctx->tx[kind], rows, ctx->group_size, 0, 0, d_err);
   cudaGraph_t graph = nullptr;
   CK(cudaStreamEndCapture(s, &graph));
   cudaGraphExec_t exec = nullptr;
@@ -1802,6 +1809,13 @@ int fwigb_set_batching(fwigb_ctx* ctx, int max_shots, unsigned long long mem_bud
 }
 
 int fwigb_last_group_count(const fwigb_ctx* ctx) { return ctx ? ctx->last_groups : -1; }
+
+int fwigb_test_inject_wait_timeout(fwigb_ctx* ctx, int enable) {
+  if (!ctx) return FWIGB_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->inject_timeout = enable != 0;
+  return FWIGB_OK;
+}
 
 int fwigb_set_illumination(fwigb_ctx* ctx, int enable) {
   if (!ctx) return FWIGB_ERR_ARG;

@@ -186,10 +186,12 @@ struct SweepGrid {
 // iteration j; shot k works on its step nSteps_k - 2 - j. Instantiated for
 // K = 1 and K = kPackShots. Each returns the number of kernels it launched.
 // The forward launchers take the rows per thread (1 or 2; the pack's maps
-// must be the matching variant).
+// must be the matching variant). launch_fwd_stress flags: bit 0 saves the
+// boundary ring of step it; bit 1 is the timeout test hook (the sweep's
+// bounded wait runs out after its tiles have landed and raises err).
 template <int K>
 int launch_fwd_stress(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
-                      int it, bool save, unsigned* err);
+                      int it, int flags, unsigned* err);
 template <int K>
 int launch_fwd_velocity(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
                         unsigned* err);

@@ -34,6 +34,8 @@ constexpr float kMega = 1.0e6f;       // MEGA (utilities.h:16)
 // Bounded waits: a sweep that waits this many polls for its staged tiles
 // gives up, raises its error word and returns instead of hanging.
 constexpr unsigned kSpinLimit = 1u << 22;
+// Polls of the injected wait of the timeout test hook (stage_wait).
+constexpr unsigned kInjectPolls = 256;
 
 // ---- mbarrier / TMA (sm_90+ PTX; issued by one thread per block) ----
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -55,8 +57,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
-  for (unsigned n = 0; n < kSpinLimit; ++n)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, unsigned limit = kSpinLimit) {
+  for (unsigned n = 0; n < limit; ++n)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -98,12 +100,24 @@ __device__ __forceinline__ void stage_begin(const TileMaps& mp, float* sm, uint6
 
 // Waits (bounded) for the staged tiles. On a timeout the error word is raised
 // and the thread waits once more so that copies still in flight land before
-// the block exits; the caller then returns without computing.
-__device__ __forceinline__ bool stage_wait(uint64_t* bar, unsigned* err) {
-  if (mbar_wait_bounded(bar, 0)) return true;
-  atomicOr(err, 1u);
-  mbar_wait_bounded(bar, 0);
-  return false;
+// the block exits; the caller then returns without computing. Should that
+// second wait run out too, copies may still land after the block has left:
+// the host then reports FWIGB_ERR_TIMEOUT for the whole call and its outputs
+// are undefined (the next run re-zeroes every field it uses).
+// `inject` (the timeout test hook): once the tiles have landed, the thread
+// also waits for the barrier's next phase, which nothing completes, so the
+// bounded wait runs out with no copy in flight and the error word is raised.
+__device__ __forceinline__ bool stage_wait(uint64_t* bar, unsigned* err, bool inject = false) {
+  if (!mbar_wait_bounded(bar, 0)) {
+    atomicOr(err, 1u);
+    mbar_wait_bounded(bar, 0);
+    return false;
+  }
+  if (inject && !mbar_wait_bounded(bar, 1, kInjectPolls)) {
+    atomicOr(err, 1u);
+    return false;
+  }
+  return true;
 }
 
 // Staggered 4th-order differences. Dm uses (i-2, i-1, i, i+1), Dp
@@ -270,7 +284,7 @@ __device__ __forceinline__ float dd(float p, float q, float s, float t, float r)
 // depths (after the staged tiles have landed).
 template <int TX, int K, int R>
 __device__ __forceinline__ void fwd_stress_edge(const SweepPack<K>& P, int shot, int z0, int x0, int it, int save,
-                                                unsigned* err) {
+                                                bool inject, unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
   SWEEP_EDGE_CELL(BOXZ, R)
@@ -281,7 +295,7 @@ __device__ __forceinline__ void fwd_stress_edge(const SweepPack<K>& P, int shot,
   const ShotD& sh = S.sh;
   const bool rec_tile = tile_meets_shot_box(sh, z0, x0, 32 * R, TX);
   const StoreD& st = S.st;
-  if (!stage_wait(&bar, err)) return;
+  if (!stage_wait(&bar, err, inject)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
   auto cell = [&](const int z, const size_t i, const int b) {
@@ -500,7 +514,7 @@ __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int 
     }
     gr.mu[i] = acc;
   }
-  // el_velocity_adj (el_velocity_adj.cu:161-206); the psi memory terms are
+  // el_velocity_adj (el_velocity_adj.cu:57-102); the psi memory terms are
   // read only where their CPML coefficient is non-zero.
   if (!in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1)) return;
   const bool zp = (z < g.nPml) || (z > g.zpml_hi);
@@ -547,7 +561,7 @@ __device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int 
 
 // C: res_injection (utilities.cu:569-580) + el_stress_adj (el_stress_adj.cu:53-97)
 //    + source_grad (utilities.cu:582-593) + el_velocity(isFor=false) with the
-//    density kernel (el_velocity.cu:220-244) + to_bnd(velocity).
+//    density kernel (el_velocity.cu:84-117) + to_bnd(velocity).
 //    Staged: vz_a, vx_a, szz, sxx, sxz.
 template <int TX, int K, int R>
 __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
@@ -660,7 +674,7 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
     f.vx[i] = vx;
   }
   // rho kernel gather: (z,x) receives A and B of itself, A of (z-1,x) and B of
-  // (z,x-1) (el_velocity.cu:238-243; the x guard of :242 is always true).
+  // (z,x-1) (el_velocity.cu:101-110; the x guard of :109 is always true).
   if (in_box(z, x, g.zi0, g.zi1, g.xi0, g.xi1 + 1)) {
     float acc = gd;
     if (x <= g.xi1) {
@@ -699,7 +713,8 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
 
 // Forward fast bodies, one depth per thread (32-row tiles).
 template <int TX, int K>
-__device__ __forceinline__ void fwd_stress_fast1(const SweepPack<K>& P, int shot, int z0, int x0, int it, unsigned* err) {
+__device__ __forceinline__ void fwd_stress_fast1(const SweepPack<K>& P, int shot, int z0, int x0, int it, bool inject,
+                                                 unsigned* err) {
   SWEEP_FAST_SLOT(kTileZ)
   SWEEP_CELL(kBoxZ, 1)
   SWEEP_SMEM(kBoxZ)
@@ -708,7 +723,7 @@ __device__ __forceinline__ void fwd_stress_fast1(const SweepPack<K>& P, int shot
   SWEEP_TMA(2, kBoxZ)
   float szz = f.szz[i], sxx = f.sxx[i];
   const float sxz = f.sxz[i];
-  if (!stage_wait(&bar, err)) return;
+  if (!stage_wait(&bar, err, inject)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
   const float dvz_dz = sdm(s_vz, b, 1, g.rdz);
@@ -765,7 +780,7 @@ __device__ __forceinline__ void fwd_velocity_fast1(const SweepPack<K>& P, int sh
 // column offset along x, which cover the stencils of both depths.
 template <int TX, int K, int R>
 __device__ __forceinline__ void fwd_stress_fast2(const SweepPack<K>& P, int shot, int z0, int x0, int it,
-                                                 unsigned* err) {
+                                                 bool inject, unsigned* err) {
   static_assert(R == 2, "the forward fast bodies handle two depths per thread");
   constexpr int TZ = 32 * R, BOXZ = TZ + 8;
   SWEEP_FAST_SLOT(TZ)
@@ -775,7 +790,7 @@ __device__ __forceinline__ void fwd_stress_fast2(const SweepPack<K>& P, int shot
   pdl_wait();
   SWEEP_TMA(2, BOXZ)
   const float2 szz = ld2(f.szz + i), sxx = ld2(f.sxx + i), sxz = ld2(f.sxz + i);
-  if (!stage_wait(&bar, err)) return;
+  if (!stage_wait(&bar, err, inject)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
   const float rdz = g.rdz, rdx = g.rdx, dt = g.dt;
@@ -1292,16 +1307,19 @@ __device__ __forceinline__ void bwd_C_fast2(const SweepPack<K>& P, int shot, int
 
 // Forward sweeps: R depths per thread (tiles of 32 R rows), R in {1, 2}
 // picked per workload by the autotuner.
+// flags: bit 0 saves the boundary ring, bit 1 is the timeout test hook
+// (stage_wait's `inject`).
 template <int TX, int K, int R>
-__global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ SweepPack<K> P, int it, int save, unsigned* err) {
+__global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ SweepPack<K> P, int it, int flags, unsigned* err) {
   SWEEP_KERNEL_TILE(32 * R)
+  const bool inject = (flags & 2) != 0;
   if (fast) {
     if constexpr (R == 1)
-      fwd_stress_fast1<TX, K>(P, shot, z0, x0, it, err);
+      fwd_stress_fast1<TX, K>(P, shot, z0, x0, it, inject, err);
     else
-      fwd_stress_fast2<TX, K, R>(P, shot, z0, x0, it, err);
+      fwd_stress_fast2<TX, K, R>(P, shot, z0, x0, it, inject, err);
   } else {
-    fwd_stress_edge<TX, K, R>(P, shot, z0, x0, it, save, err);
+    fwd_stress_edge<TX, K, R>(P, shot, z0, x0, it, flags & 1, inject, err);
   }
 }
 
@@ -1766,8 +1784,8 @@ dim3 sweep_grid(int tx, int tz, const SweepGrid& gr, int nshots) {
 
 template <int K>
 int launch_fwd_stress(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int it,
-                      bool save, unsigned* err) {
-  const int sv = save ? 1 : 0;
+                      int flags, unsigned* err) {
+  const int sv = flags & 3;
   if (rows == 2)
     FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_stress<TX, K, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZFwd>(2), s, p, it, sv, err))
@@ -1814,7 +1832,7 @@ int launch_bwd_C(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int ns
 }
 
 #define FWIGB_INSTANTIATE(K)                                                                                    \
-  template int launch_fwd_stress<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&, int, bool, \
+  template int launch_fwd_stress<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&, int, int,  \
                                     unsigned*);                                                                  \
   template int launch_fwd_velocity<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&,        \
                                       unsigned*);                                                                \

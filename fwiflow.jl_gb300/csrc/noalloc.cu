@@ -10,7 +10,12 @@
 // double per receiver trace plus the total, lives in the file-scope device
 // array below. Its address is looked up once per device, by the first call
 // made with that device current, so make that first call before any stream
-// capture.
+// capture on that device. Each call synchronises its stream to return the
+// misfit to the host.
+//
+// It reproduces the plain residual path of fwigb_misfit only: the fixed 0.005
+// data taper, without per-trace windows, band-pass filter or source-wavelet
+// update.
 //
 // The array holds kNoAllocMaxTraces + 1 doubles (512 KiB + 8 B). Every GPU that
 // loads the library keeps it until the process exits. All calls share it:
@@ -130,8 +135,11 @@ int fwigb_misfit_gathers_noalloc(const float* d_obs, float* d_syn, float* d_res,
     t_noalloc_err = "nrec must be between 1 and 65536 (the size of the static misfit scratch)";
     return FWIGB_ERR_ARG;
   }
-  if (2.0 * (nSteps * dt * 0.005f) >= nSteps * dt) {
-    t_noalloc_err = "nSteps too small for the data taper";
+  // The taper's ramps span nSteps * dt * 0.005 seconds at each end of the
+  // record; a zero (underflowed) or non-finite span would divide by zero.
+  const float record = static_cast<float>(nSteps) * dt;
+  if (!std::isfinite(record) || !(record * 0.005f > 0.0f)) {
+    t_noalloc_err = "nSteps * dt gives no usable data taper (its ramp nSteps * dt * 0.005 must be positive and finite)";
     return FWIGB_ERR_ARG;
   }
   int st = FWIGB_OK;

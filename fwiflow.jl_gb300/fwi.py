@@ -189,6 +189,12 @@ class FwiContext:
     def last_group_count(self) -> int:
         return int(self._lib.fwigb_last_group_count(self._h))
 
+    def test_inject_wait_timeout(self, enable: bool) -> None:
+        """Failure-path test hook: while enabled, every run's first forward
+        sweep lets its bounded wait run out and the call raises FwiError with
+        status ERR_TIMEOUT; the context stays usable."""
+        _lib.check(self._lib.fwigb_test_inject_wait_timeout(self._h, int(enable)), self._h)
+
     def set_illumination(self, enable: bool = True) -> None:
         """Accumulate the source illumination sum_t (vz^2 + vx^2) in the
         following runs (all their shots)."""

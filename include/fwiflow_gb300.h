@@ -44,7 +44,7 @@ typedef enum fwigb_status {
   FWIGB_ERR_CUDA = 4,       /* CUDA runtime error */
   FWIGB_ERR_OOM = 5,        /* device allocation failed */
   FWIGB_ERR_IO = 6,         /* observed-data or output file I/O failed */
-  FWIGB_ERR_TIMEOUT = 7,    /* a bounded device wait gave up */
+  FWIGB_ERR_TIMEOUT = 7,    /* a bounded device wait gave up: the call's outputs are undefined */
   FWIGB_ERR_UNSUPPORTED = 8 /* option of the parameter file this build does not implement */
 } fwigb_status;
 
@@ -162,6 +162,14 @@ int fwigb_last_group_count(const fwigb_ctx *ctx);
 int fwigb_set_illumination(fwigb_ctx *ctx, int enable);
 int fwigb_fetch_illumination(fwigb_ctx *ctx, double *illum);
 
+/* Test hook of the failure path (no counterpart in the reference, which has
+ * no bounded waits): with enable != 0, the first forward sweep of every
+ * following run waits, once its staged tiles have landed, for a barrier
+ * phase that nothing completes; its bounded wait runs out, the run returns
+ * FWIGB_ERR_TIMEOUT, and the context stays usable. No copy is in flight when
+ * the wait gives up. Off by default. */
+int fwigb_test_inject_wait_timeout(fwigb_ctx *ctx, int enable);
+
 /* Tile widths (columns per thread block: 4, 8 or 16) of the four sweeps
  * (forward stress, forward velocity, backward B, backward C). By default an
  * autotuner times every width and 1 or 2 depths per thread on the context's
@@ -201,15 +209,20 @@ int fwigb_kernel_times(fwigb_ctx *ctx, double *total_ms, long long *launches);
  * For callers that cannot call cudaMalloc: an operator inside a framework that
  * owns the device memory pool (TensorFlow's allocator, as for FwiFlow's own TF
  * op; an XLA / JAX runtime that reserved the GPU), or a service with a fixed
- * device-memory budget. Computes what fwigb_misfit computes for one shot from
- * gathers the caller already holds on the device: d_obs, d_syn and d_res are
- * device buffers [nrec][nSteps] float with 1 <= nrec <= 65536; d_syn is tapered
- * in place, d_res receives the adjoint source, *misfit (host) the misfit.
+ * device-memory budget. For one shot whose gathers the caller already holds on
+ * the device, computes the misfit and the adjoint source of fwigb_misfit's
+ * plain residual path: the fixed 0.005 data taper, with no per-trace windows
+ * (if_win), no band-pass filter and no source-wavelet update; with any of
+ * those options on, fwigb_misfit's results differ from this call's.
+ * d_obs, d_syn and d_res are device buffers [nrec][nSteps] float with
+ * 1 <= nrec <= 65536; d_syn is tapered in place, d_res receives the adjoint
+ * source, *misfit (host) the misfit.
  * The only scratch is a static device array of 65537 doubles that every GPU
  * loading the library keeps until exit; all calls share it, so calls that
  * overlap on the GPU race. The first call on a device (with that device
- * current) looks up the array's address: make it before any stream capture.
- * Synchronises `stream` (a cudaStream_t; NULL for the legacy default stream).
+ * current) looks up the array's address: make that first call before any
+ * stream capture on the device. Each call synchronises `stream` (a
+ * cudaStream_t; NULL for the legacy default stream) to return the misfit.
  * Allocates nothing. */
 int fwigb_misfit_gathers_noalloc(const float *d_obs, float *d_syn, float *d_res, int nrec, int nSteps, float dt,
                                  double *misfit, void *stream);

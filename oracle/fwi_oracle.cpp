@@ -10,7 +10,7 @@
 //   el_stress        (el_stress.cu:24-133)       forward + reverse/imaging
 //   el_velocity      (el_velocity.cu:20-118)     forward + reverse/imaging
 //   el_stress_adj    (el_stress_adj.cu:22-104)
-//   el_velocity_adj  (el_velocity_adj.cu:22-108)
+//   el_velocity_adj  (el_velocity_adj.cu:22-107)
 //   add_source, recording, res_injection, source_grad (utilities.cu:506-593)
 //   from_bnd / to_bnd boundary strips (utilities.cu:361-424, Boundary.cu:5-102)
 //   cuda_window (both overloads), gpuMinus, cuda_cal_objective (utilities.cu:154-205, 653-747)
@@ -338,7 +338,7 @@ void stress_reverse(const Grid& g, const Media& m, Fields& f, std::vector<float>
   }
 }
 
-// el_velocity_adj (el_velocity_adj.cu:22-108): adjoint of the velocity/CPML step.
+// el_velocity_adj (el_velocity_adj.cu:22-107): adjoint of the velocity/CPML step.
 void velocity_adjoint(const Grid& g, const Media& m, const Cpml& c, Fields& f) {
   const int nz = g.nz, nx = g.nx, nPml = g.nPml, nPad = g.nPad;
   const float dz = g.dz, dx = g.dx, dt = g.dt;
