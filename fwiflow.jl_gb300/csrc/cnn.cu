@@ -594,6 +594,7 @@ extern "C" {
 int fwigb_cnn_conv3x3(const void* x, int Hz, int Wx, int cin_pad, int cout_pad, int epilogue, const void* wfrag,
                       const float* bias, void* y_bf16, float* y_f32, void* z_pre, const void* z_prev,
                       void* stream) {
+  cudaGetLastError();  // drop a stale non-sticky error of an earlier, unrelated call
   if (!x || !wfrag || Hz <= 0 || Wx <= 0 || Hz % kTz != 0) return FWIGB_ERR_ARG;
   if (epilogue == kEpiGelu && (!bias || !y_bf16 || !z_pre)) return FWIGB_ERR_ARG;
   if (epilogue == kEpiLinearF32 && (!bias || !y_f32)) return FWIGB_ERR_ARG;
@@ -620,6 +621,7 @@ int fwigb_cnn_conv3x3(const void* x, int Hz, int Wx, int cin_pad, int cout_pad, 
 
 int fwigb_cnn_wgrad_partials(const void* x, const void* dz, int Hz, int Wx, int cin_pad, int cout_pad,
                              float* partials, void* stream) {
+  cudaGetLastError();  // drop a stale non-sticky error of an earlier, unrelated call
   if (!x || !dz || !partials || Hz <= 0 || Wx <= 0 || Hz % kTz != 0) return FWIGB_ERR_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const dim3 grid(Hz / kTz, (Wx + kTx - 1) / kTx);
@@ -641,6 +643,7 @@ int fwigb_cnn_tile_count(int Hz, int Wx) { return (Hz / kTz) * ((Wx + kTx - 1) /
 int fwigb_cnn_conv3x3_tc(const void* x, int Hz, int Wx, int cin_pad, int epilogue, const void* wpack,
                          const float* bias, void* y_bf16, void* z_pre, const void* z_prev, unsigned* err_word,
                          void* stream) {
+  cudaGetLastError();  // drop a stale non-sticky error of an earlier, unrelated call
   if (!x || !wpack || !y_bf16 || !err_word || Hz <= 0 || Wx <= 0) return FWIGB_ERR_ARG;
   if (epilogue == kEpiGelu && (!bias || !z_pre)) return FWIGB_ERR_ARG;
   if (epilogue == kEpiDGelu && !z_prev) return FWIGB_ERR_ARG;
@@ -671,6 +674,7 @@ int fwigb_cnn_conv3x3_tc(const void* x, int Hz, int Wx, int cin_pad, int epilogu
 
 int fwigb_cnn_pack_weights_tc(const float* w, int cin, int cout, int cin_pad, int cout_pad, int transposed,
                               void* pack, void* stream) {
+  cudaGetLastError();  // drop a stale non-sticky error of an earlier, unrelated call
   if (!w || !pack || cin <= 0 || cout <= 0 || cin > cin_pad || cout > cout_pad) return FWIGB_ERR_ARG;
   const int kin = transposed ? cout_pad : cin_pad, nout = transposed ? cin_pad : cout_pad;
   if ((kin != 16 && kin != 32) || nout != 32) return FWIGB_ERR_UNSUPPORTED;
@@ -681,12 +685,14 @@ int fwigb_cnn_pack_weights_tc(const float* w, int cin, int cout, int cin_pad, in
 }
 
 int fwigb_cnn_reduce_partials(const float* partials, int nblocks, int n, float* out, void* stream) {
+  cudaGetLastError();  // drop a stale non-sticky error of an earlier, unrelated call
   if (!partials || !out || nblocks <= 0 || n <= 0) return FWIGB_ERR_ARG;
   k_reduce_partials<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(partials, nblocks, n, out);
   return cudaGetLastError() == cudaSuccess ? FWIGB_OK : FWIGB_ERR_CUDA;
 }
 
 int fwigb_cnn_bias_partials(const void* dz, long long npix, int c_pad, int chunk, float* partials, void* stream) {
+  cudaGetLastError();  // drop a stale non-sticky error of an earlier, unrelated call
   if (!dz || !partials || npix <= 0 || chunk <= 0) return FWIGB_ERR_ARG;
   const int nb = static_cast<int>((npix + chunk - 1) / chunk);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -702,6 +708,7 @@ int fwigb_cnn_bias_partials(const void* dz, long long npix, int c_pad, int chunk
 
 int fwigb_cnn_adam(float* w, const float* grad, float* m1, float* m2, int n, float lr, float beta1, float beta2,
                    float eps, int step, void* stream) {
+  cudaGetLastError();  // drop a stale non-sticky error of an earlier, unrelated call
   if (!w || !grad || !m1 || !m2 || n <= 0 || step <= 0) return FWIGB_ERR_ARG;
   const float c1 = 1.0f - powf(beta1, static_cast<float>(step));
   const float c2 = 1.0f - powf(beta2, static_cast<float>(step));
@@ -712,6 +719,7 @@ int fwigb_cnn_adam(float* w, const float* grad, float* m1, float* m2, int n, flo
 
 int fwigb_cnn_pack_weights(const float* w, int cin, int cout, int cin_pad, int cout_pad, int transposed, void* frag,
                            void* stream) {
+  cudaGetLastError();  // drop a stale non-sticky error of an earlier, unrelated call
   if (!w || !frag || cin <= 0 || cout <= 0 || cin > cin_pad || cout > cout_pad) return FWIGB_ERR_ARG;
   const int kin = transposed ? cout_pad : cin_pad, nout = transposed ? cin_pad : cout_pad;
   if (kin % 16 != 0 || nout % 8 != 0) return FWIGB_ERR_ARG;
@@ -723,6 +731,7 @@ int fwigb_cnn_pack_weights(const float* w, int cin, int cout, int cin_pad, int c
 
 int fwigb_cnn_mse_grad(const float* y, const float* target, const float* mask, long long npix, int c_pad, int nc,
                        float inv_count, void* dy, float* partials, void* stream) {
+  cudaGetLastError();  // drop a stale non-sticky error of an earlier, unrelated call
   if (!y || !target || !mask || !dy || !partials || npix <= 0 || nc > c_pad) return FWIGB_ERR_ARG;
   const int nb = static_cast<int>((npix + 255) / 256);
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -378,7 +378,10 @@ struct DevBuf {
     p = nullptr;
     bytes = 0;
     cudaError_t e = cudaMalloc(&p, n);
-    if (e == cudaSuccess) bytes = n;
+    if (e == cudaSuccess)
+      bytes = n;
+    else
+      cudaGetLastError();  // a failed allocation is reported here, not by the next launch check
     return e;
   }
   void release() {
@@ -657,12 +660,19 @@ int open_ctx(const char* para_fname, int device, fwigb_ctx* ctx) {
   return setup_geometry(ctx);
 }
 
+// Drops a non-sticky error that an earlier, unrelated CUDA call of this host
+// thread left behind (a failed allocation, say), so that this call's own
+// launch checks report only this call's failures. Sticky errors (a corrupted
+// context) persist and are still reported by the next call that fails.
+void clear_stale_error() { cudaGetLastError(); }
+
 int set_model(fwigb_ctx* ctx, const double* lam, const double* mu, const double* den) {
   if (!lam || !mu || !den) {
     ctx->err = "null model array";
     return FWIGB_ERR_ARG;
   }
   CK(cudaSetDevice(ctx->device));
+  clear_stale_error();
   const size_t nh = ctx->ncell, n = ctx->cells;
   const int ldz = ctx->geo.ldz;
   double* st = ctx->stage.as<double>();
@@ -1248,6 +1258,7 @@ int run(fwigb_ctx* ctx, int calc_id) {
     return FWIGB_ERR_ARG;
   }
   CK(cudaSetDevice(ctx->device));
+  clear_stale_error();
   std::vector<std::vector<int>> groups;
   TRY_RC(plan_groups(ctx, adj, groups));
   cudaStream_t s = ctx->stream;

@@ -146,6 +146,7 @@ int fwigb_misfit_gathers_noalloc(const float* d_obs, float* d_syn, float* d_res,
   double* scratch = scratch_for_current_device(&st);
   if (!scratch) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaGetLastError();  // drop a stale non-sticky error of an earlier, unrelated call of this thread
   k_trace_residual<<<nrec, 256, 0, s>>>(d_obs, d_syn, d_res, nSteps, dt, scratch);
   k_sum_traces<<<1, 32, 0, s>>>(scratch, nrec, kNoAllocMaxTraces);
   cudaError_t e = cudaGetLastError();

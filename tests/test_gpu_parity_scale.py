@@ -11,8 +11,13 @@
   1120x3152 cells, dx 5 m, dt 0.5 ms, 3072 receivers) on one shot with a
   600-step record.
 Tolerances as in the other parity tests: gathers and misfit 1e-4 relative L2,
-gradients 1e-3 (FP32). The oracle runs on all host cores (tens of seconds per
-case).
+gradients 1e-3 (FP32). The source-wavelet gradient is the adjoint field at one
+cell after thousands of FP32 steps, a much less averaged quantity than the
+model gradients: its bar is max(1e-3, 4 x the case's FP32 floor), the floor
+being how far the oracle built with FP32 arithmetic only lies from the
+reference-precision oracle on the same case (5.6e-3 on the dipping model,
+against ~1e-6 for the model gradients), computed live as in the golden tests.
+The oracle runs on all host cores (tens of seconds per case).
 """
 import numpy as np
 import pytest
@@ -35,13 +40,16 @@ def _parity(fw, orc, w, para, ids, check_stf=True):
         assert rel(a, b) < TOL_DATA, ("gathers", k, rel(a, b))
     lam, mu, rho = w.moduli()
     o = orc.cufd(1, lam, mu, rho, w.stf, ids, para, obs=ref_obs)
+    o["misfit"] = orc.cufd(0, lam, mu, rho, w.stf, ids, para, obs=ref_obs)["misfit"]  # (calc_id 1 returns none)
     J, gl, gm, gd, gs = ctx.misfit_grad(lam, mu, rho, w.stf, ids, obs=ref_obs)
     assert abs(J - o["misfit"]) <= TOL_DATA * abs(o["misfit"]), (J, o["misfit"])
     for k, a in (("g_lambda", gl), ("g_mu", gm), ("g_den", gd)):
         assert rel(a, o[k]) < TOL_GRAD, (k, rel(a, o[k]))
     if check_stf:  # (ids are 0 .. n-1 here: the oracle's row of shot i is row i)
+        o32 = orc.cufd(1, lam, mu, rho, w.stf, ids, para, obs=ref_obs, precision="fp32")
         for i in range(len(ids)):
-            assert rel(gs[i], o["g_stf"][i]) < TOL_GRAD, ("g_stf", i)
+            tol = max(TOL_GRAD, 4.0 * rel(o32["g_stf"][i], o["g_stf"][i]))
+            assert rel(gs[i], o["g_stf"][i]) < tol, ("g_stf", i, rel(gs[i], o["g_stf"][i]), tol)
     return ctx, ref_obs, o, (J, gl, gm, gd)
 
 
