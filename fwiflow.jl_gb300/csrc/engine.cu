@@ -565,6 +565,7 @@ Geo make_geo(const Params& p, int nx, const float* zprof, const float* xprof) {
   g.dt = p.dt;
   g.rdz = 1.0f / p.dz;
   g.rdx = 1.0f / p.dx;
+  g.zact1 = std::max(g.zs1, g.rz1);
   // An adjoint psi memory cell matters only within 2 cells of a cell whose
   // CPML coefficient a (or a_half) is non-zero; elsewhere the reference's
   // updates (el_stress_adj.cu:68-94) are multiplied by a == 0.
@@ -613,6 +614,23 @@ Geo make_geo(const Params& p, int nx, const float* zprof, const float* xprof) {
            x < g.xband_hi && x >= g.xi0 + 1 && x <= g.xi1 && x >= g.rx0 + 5 && x <= g.rx1 - 5 && Kx[x] == 1.0f &&
            Kxh[x] == 1.0f && ax[x] == 0.0f && axh[x] == 0.0f;
   }, g.fx0, g.fx1);
+  // Mid box: stencil domain without any CPML cell (K = 1, a = 0); it holds
+  // the fast box plus the ring, band and interior-guard cells next to it.
+  run(p.nz, [&](int z) {
+    return z >= g.zs0 && z <= g.zs1 && z >= g.nPml && z <= g.zpml_hi && Kz[z] == 1.0f && Kzh[z] == 1.0f &&
+           az[z] == 0.0f && azh[z] == 0.0f;
+  }, g.mz0, g.mz1);
+  run(nx, [&](int x) {
+    return x >= g.xs0 && x <= g.xs1 && x >= g.nPml && x <= g.xpml_hi_s && x <= g.xpml_hi_v && Kx[x] == 1.0f &&
+           Kxh[x] == 1.0f && ax[x] == 0.0f && axh[x] == 0.0f;
+  }, g.mx0, g.mx1);
+  if (g.fz0 <= g.fz1 && g.fx0 <= g.fx1 &&
+      !(g.mz0 <= g.fz0 && g.fz1 <= g.mz1 && g.mx0 <= g.fx0 && g.fx1 <= g.mx1)) {
+    g.mz0 = g.fz0;  // (never on the reference's grids) no mid tiles
+    g.mz1 = g.fz1;
+    g.mx0 = g.fx0;
+    g.mx1 = g.fx1;
+  }
   return g;
 }
 
@@ -1099,8 +1117,14 @@ int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
   ctx->npacks = (G + kPackShots - 1) / kPackShots;
   ctx->pack_nx.assign(ctx->npacks, 0);
   for (int k = 0; k < G; ++k) ctx->pack_nx[k / kPackShots] = std::max(ctx->pack_nx[k / kPackShots], slots[k].g.nx);
-  ctx->pack_grid.assign(ctx->npacks, SweepGrid{ctx->p.nz, 0});
+  // Launch extents: the widest member sub-grid, and rows down to the last
+  // one a sweep touches (zact1, or the lowest source / receiver row).
+  ctx->pack_grid.assign(ctx->npacks, SweepGrid{0, 0});
   for (int q = 0; q < ctx->npacks; ++q) ctx->pack_grid[q].nx = ctx->pack_nx[q];
+  for (int k = 0; k < G; ++k) {
+    const int rows = std::min(slots[k].g.nz, std::max(slots[k].g.zact1, slots[k].sh.rbz1) + 1);
+    ctx->pack_grid[k / kPackShots].nz = std::max(ctx->pack_grid[k / kPackShots].nz, rows);
+  }
   if (G == 1) {
     ctx->pack1.assign(kSweepVariants * 3, SweepPack<1>{});
     for (int w = 0; w < kSweepVariants * 3; ++w) {

@@ -56,14 +56,26 @@ struct Geo {
   // the adjoint memory bands and the boundary ring, and with K = 1, a = 0 in
   // both CPML profiles. Empty when fz0 > fz1 or fx0 > fx1.
   int fz0, fz1, fx0, fx1;
+  // Mid box: cells of the stencil domain outside the CPML (K = 1, a = 0 in
+  // both profiles); it holds the fast box. Tiles inside it but not inside the
+  // fast box (the ring, adjoint-memory band and interior-guard cells next to
+  // the CPML) run the mid form of a sweep: the fast arithmetic with per-cell
+  // ring, band and guard handling.
+  int mz0, mz1, mx0, mx1;
+  // Last row any sweep reads its own cells of or writes, apart from the
+  // shot's source and receivers: max(zs1, rz1). Rows below it (the nPad rows
+  // past the stencil domain) are only read as halo.
+  int zact1;
   float dt, rdz, rdx;
 };
 
 // Split of a sub-grid's tiles (tz depths x tx columns, ntz x ntx in all)
 // into the fast tiles, the rectangle [ftz0, ftz1) x [ftx0, ftx1) of tiles
-// inside the fast box, and the edge tiles around it.
+// inside the fast box, the mid tiles, those of the rectangle [mtz0, mtz1) x
+// [mtx0, mtx1) inside the mid box that are not fast, and the edge tiles
+// around them.
 struct TileSplit {
-  int ntz, ntx, ftz0, ftz1, ftx0, ftx1;
+  int ntz, ntx, ftz0, ftz1, ftx0, ftx1, mtz0, mtz1, mtx0, mtx1;
 };
 
 __host__ __device__ inline TileSplit tile_split(const Geo& g, int tx, int tz) {
@@ -75,6 +87,11 @@ __host__ __device__ inline TileSplit tile_split(const Geo& g, int tx, int tz) {
   s.ftx0 = (g.fx0 + tx - 1) / tx;
   s.ftx1 = (g.fx1 + 1) / tx;
   if (g.fz0 > g.fz1 || g.fx0 > g.fx1 || s.ftz1 <= s.ftz0 || s.ftx1 <= s.ftx0) s.ftz0 = s.ftz1 = s.ftx0 = s.ftx1 = 0;
+  s.mtz0 = (g.mz0 + tz - 1) / tz;
+  s.mtz1 = (g.mz1 + 1) / tz;
+  s.mtx0 = (g.mx0 + tx - 1) / tx;
+  s.mtx1 = (g.mx1 + 1) / tx;
+  if (g.mz0 > g.mz1 || g.mx0 > g.mx1 || s.mtz1 <= s.mtz0 || s.mtx1 <= s.mtx0) s.mtz0 = s.mtz1 = s.mtx0 = s.mtx1 = 0;
   return s;
 }
 
@@ -173,9 +190,10 @@ static_assert(sizeof(SweepPack<kPackShots>) < 32000, "sweep pack exceeds the ker
 // cuTensorMapEncodeTiled). Returns false with a message on failure.
 bool encode_sweep_maps(const Geo& g, const Fields& f, int tx, SweepMaps& out, const char** err);
 
-// Launch extent of one sweep over the first shots of a pack: the largest
-// sub-grid among them (nz x nx cells). Blocks past a shot's own grid leave
-// at once.
+// Launch extent of one sweep over the first shots of a pack: the widest
+// sub-grid among them (nx), and the rows down to the last one any of them
+// touches (nz: zact1 + 1, or further down to the lowest source or receiver).
+// Blocks past a shot's own grid leave at once.
 struct SweepGrid {
   int nz, nx;
 };

@@ -150,6 +150,21 @@ __device__ __forceinline__ int ring_index(const Geo& g, int z, int x) {
   return -1;
 }
 
+// from_bnd of step it for cell (z, x) when it lies in the ring: the stresses
+// before the step's update and the velocities of the staged tile
+// (Boundary.cu:55-76).
+__device__ __forceinline__ void ring_save(const Geo& g, const StoreD& st, int it, int z, int x, float szz, float sxz,
+                                          float sxx, float vz, float vx) {
+  const int k = ring_index(g, z, x);
+  if (k < 0) return;
+  float* p = st.base + static_cast<size_t>(it) * 5 * g.ring_len + k;
+  p[0] = szz;
+  p[g.ring_len] = sxz;
+  p[2 * g.ring_len] = sxx;
+  p[3 * g.ring_len] = vz;
+  p[4 * g.ring_len] = vx;
+}
+
 // a / K of the CPML formulas, with the division skipped where K == 1 (exact:
 // a / 1 == a), i.e. everywhere outside the CPML.
 __device__ __forceinline__ float kdiv(float a, float K) { return K == 1.0f ? a : a / K; }
@@ -174,9 +189,13 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
 // the shot (its slot holds its sub-grid, fields, source, receivers and TMA
 // maps), blockIdx.x / blockIdx.y the tile of TZ depths x TX columns. A tile
 // inside the shot's fast rectangle runs the sweep's fast body (the interior
-// form of the reference kernels); any other tile runs its edge body (the
-// full CPML / boundary-ring / band logic). The choice is uniform per block.
-// Blocks past a narrower shot's grid leave before staging anything. Block
+// form of the reference kernels); a tile inside the mid rectangle (no CPML
+// cell) runs the fast body with per-cell ring, band and guard handling; any
+// other tile runs its edge body (the full CPML / boundary-ring / band
+// logic). The choice is uniform per block. Blocks past a narrower shot's grid
+// leave before staging anything, and so do blocks whose tile lies wholly
+// below row zact1 (the nPad rows, where no sweep reads or writes a cell of
+// its own) unless it holds the shot's source or a receiver. Block
 // (32, TX): lane threadIdx.x covers R adjacent depths (R = TZ / 32),
 // threadIdx.y the column; `b` is the index of its first cell in a staged box
 // (column stride BOXZ = TZ + 8).
@@ -193,11 +212,16 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
   const int z0 = blockIdx.x * (TZ_), x0 = blockIdx.y * TX;                     \
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");              \
   if (z0 >= g0.nz || x0 >= g0.nx) return;                                      \
+  if (z0 > g0.zact1 && !tile_meets_shot_box(P.slots[shot].sh, z0, x0, (TZ_), TX)) return; \
   const TileSplit ts = tile_split(g0, TX, (TZ_));                              \
   const bool fast = static_cast<int>(blockIdx.x) >= ts.ftz0 &&                 \
                     static_cast<int>(blockIdx.x) < ts.ftz1 &&                  \
                     static_cast<int>(blockIdx.y) >= ts.ftx0 &&                 \
-                    static_cast<int>(blockIdx.y) < ts.ftx1;
+                    static_cast<int>(blockIdx.y) < ts.ftx1;                    \
+  const bool mid = !fast && static_cast<int>(blockIdx.x) >= ts.mtz0 &&         \
+                   static_cast<int>(blockIdx.x) < ts.mtz1 &&                   \
+                   static_cast<int>(blockIdx.y) >= ts.mtx0 &&                  \
+                   static_cast<int>(blockIdx.y) < ts.mtx1;
 
 #define SWEEP_BODY_SLOT()                                                      \
   const ShotSlot& S = P.slots[shot];                                           \
@@ -350,7 +374,7 @@ __device__ __forceinline__ void fwd_stress_edge(const SweepPack<K>& P, int shot,
     }
     // The velocity sweep that follows does not change the stresses, so the
     // sample of step it+1 is taken here.
-    if (rec_tile) {
+    if (rec_tile && z >= sh.rbz0 && z <= sh.rbz1) {
       const int2 rr = bin_range(sh, z, x);
       for (int k = rr.x; k < rr.y; ++k) {
         const int r = sh.blk_rec[k];
@@ -606,7 +630,7 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
   float vz = p_vz[r], vx = p_vx[r], gd = p_gd[r];
   const bool dom = in_box(z, x, g.zs0, g.zs1, g.xs0, g.xs1);
   bool injected = false;
-  if (rec_tile) {
+  if (rec_tile && z >= sh.rbz0 && z <= sh.rbz1) {
     const int2 rr = bin_range(sh, z, x);
     for (int k = rr.x; k < rr.y; ++k) {
       const int r = sh.blk_rec[k];
@@ -712,9 +736,11 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
 // the edge kernels.
 
 // Forward fast bodies, one depth per thread (32-row tiles).
-template <int TX, int K>
-__device__ __forceinline__ void fwd_stress_fast1(const SweepPack<K>& P, int shot, int z0, int x0, int it, bool inject,
-                                                 unsigned* err) {
+// MID: the tile is a mid tile (no CPML cell; it may hold ring cells), and
+// the boundary ring of step it is saved when `save` is set.
+template <int TX, int K, bool MID>
+__device__ __forceinline__ void fwd_stress_fast1(const SweepPack<K>& P, int shot, int z0, int x0, int it, int save,
+                                                 bool inject, unsigned* err) {
   SWEEP_FAST_SLOT(kTileZ)
   SWEEP_CELL(kBoxZ, 1)
   SWEEP_SMEM(kBoxZ)
@@ -726,6 +752,11 @@ __device__ __forceinline__ void fwd_stress_fast1(const SweepPack<K>& P, int shot
   if (!stage_wait(&bar, err, inject)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
+  if constexpr (MID) {
+    if (save) ring_save(g, S.st, it, z, x, szz, sxz, sxx, s_vz[b], s_vx[b]);
+  } else {
+    (void)save;
+  }
   const float dvz_dz = sdm(s_vz, b, 1, g.rdz);
   const float dvx_dx = sdm(s_vx, b, kBoxZ, g.rdx);
   const float dvx_dz = sdp(s_vx, b, 1, g.rdz);
@@ -738,11 +769,13 @@ __device__ __forceinline__ void fwd_stress_fast1(const SweepPack<K>& P, int shot
       szz += sh.src_szz[it];
       sxx += sh.src_sxx[it];
     }
-    const int2 rr = bin_range(sh, z, x);
-    for (int k = rr.x; k < rr.y; ++k) {
-      const int r = sh.blk_rec[k];
-      if (sh.rec_z[r] == z && sh.rec_x[r] == x)
-        sh.data[static_cast<size_t>(r) * sh.nSteps + it + 1] = szz + 3.0f * sxx;
+    if (z >= sh.rbz0 && z <= sh.rbz1) {
+      const int2 rr = bin_range(sh, z, x);
+      for (int k = rr.x; k < rr.y; ++k) {
+        const int r = sh.blk_rec[k];
+        if (sh.rec_z[r] == z && sh.rec_x[r] == x)
+          sh.data[static_cast<size_t>(r) * sh.nSteps + it + 1] = szz + 3.0f * sxx;
+      }
     }
   }
   f.szz[i] = szz;
@@ -778,8 +811,8 @@ __device__ __forceinline__ void fwd_velocity_fast1(const SweepPack<K>& P, int sh
 // operands and results move as float2, and the staged samples are read in
 // pairs (b-2, b-1), (b, b+1), (b+2, b+3) along z and (b, b+1) at each
 // column offset along x, which cover the stencils of both depths.
-template <int TX, int K, int R>
-__device__ __forceinline__ void fwd_stress_fast2(const SweepPack<K>& P, int shot, int z0, int x0, int it,
+template <int TX, int K, int R, bool MID>
+__device__ __forceinline__ void fwd_stress_fast2(const SweepPack<K>& P, int shot, int z0, int x0, int it, int save,
                                                  bool inject, unsigned* err) {
   static_assert(R == 2, "the forward fast bodies handle two depths per thread");
   constexpr int TZ = 32 * R, BOXZ = TZ + 8;
@@ -793,6 +826,14 @@ __device__ __forceinline__ void fwd_stress_fast2(const SweepPack<K>& P, int shot
   if (!stage_wait(&bar, err, inject)) return;
   const float* s_vz = sm;
   const float* s_vx = sm + N;
+  if constexpr (MID) {
+    if (save) {
+      ring_save(g, S.st, it, z, x, szz.x, sxz.x, sxx.x, s_vz[b], s_vx[b]);
+      ring_save(g, S.st, it, z + 1, x, szz.y, sxz.y, sxx.y, s_vz[b + 1], s_vx[b + 1]);
+    }
+  } else {
+    (void)save;
+  }
   const float rdz = g.rdz, rdx = g.rdx, dt = g.dt;
   const float2 zm = ld2(s_vz + b - 2), z0v = ld2(s_vz + b), zp = ld2(s_vz + b + 2);
   const float2 xm = ld2(s_vx + b - 2), x0v = ld2(s_vx + b), xp = ld2(s_vx + b + 2);
@@ -819,6 +860,7 @@ __device__ __forceinline__ void fwd_stress_fast2(const SweepPack<K>& P, int shot
         *szr[r] += sh.src_szz[it];
         *sxr[r] += sh.src_sxx[it];
       }
+      if (zr < sh.rbz0 || zr > sh.rbz1) continue;
       const int2 rr = bin_range(sh, zr, x);
       for (int k = rr.x; k < rr.y; ++k) {
         const int q = sh.blk_rec[k];
@@ -896,7 +938,10 @@ __device__ __forceinline__ void str(float* p, const float (&v)[R]) {
 // the own-cell operands of all R depths are loaded before the staged tiles
 // are awaited; the depths are then computed in turn (the stencil samples
 // two depths share are read once after unrolling).
-template <int TX, int K, int R>
+// MID: a mid tile (no CPML cell): the reverse stress update and the lambda
+// term only at cells of the reverse-time interior, the ring's stresses of
+// step it restored, and the mu gathers with the guards of the edge form.
+template <int TX, int K, int R, bool MID>
 __device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int TZ = 32 * R, BOXZ = TZ + 8;
   SWEEP_FAST_SLOT(TZ)
@@ -932,39 +977,70 @@ __device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int 
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int bb = b + r;
+    const int zr = z + r;
     const float hz = r == 0 ? hz0 : h[r - 1];     // hs at (z-1, x)
     const float hzx = r == 0 ? hzx0 : hx[r - 1];  // hs at (z-1, x-1)
-    if (special && z + r == sh.src_z && x == sh.src_x) {
+    if (special && zr == sh.src_z && x == sh.src_x) {
       szz[r] -= sh.src_szz_r[it];
       sxx[r] -= sh.src_sxx_r[it];
     }
+    const bool inter = !MID || in_box(zr, x, g.zi0, g.zi1, g.xi0, g.xi1);
     const float dvz_dz = sdm(s_vz, bb, 1, g.rdz);
     const float dvx_dx = sdm(s_vx, bb, BOXZ, g.rdx);
     const float dvx_dz = sdp(s_vx, bb, 1, g.rdz);
     const float dvz_dx = sdp(s_vz, bb, BOXZ, g.rdx);
-    o_szz[r] = szz[r] - (l2m[r] * dvz_dz + lam[r] * dvx_dx) * dt;
-    o_sxx[r] = sxx[r] - (lam[r] * dvz_dz + l2m[r] * dvx_dx) * dt;
-    const float e_own = dvx_dz + dvz_dx;
-    o_sxz[r] = sxz[r] - amu[r] * e_own * dt;
-    const float sa = s_szz_a[bb], xa = s_sxx_a[bb];
-    o_gl[r] = gl[r] + -(sa + xa) * (dvz_dz + dvx_dx) * dt * kMega;
-    const float gmu_own = (-2.0f * sa * dvz_dz * dt - 2.0f * xa * dvx_dx * dt) * kMega;
-    // mu kernel: own term and the three neighbouring 2x2 blocks (all guards hold).
-    float acc = gm[r] + gmu_own;
-    if (h[r] != 0.0f) acc += w[r] * (-s_sxz_a[bb] * e_own * dt * h[r]);
-    if (hz != 0.0f) {
-      const int bj = bb - 1;
-      acc += w[r] * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, BOXZ, g.rdx)) * dt * hz);
+    float e_own = 0.0f, gmu_own = 0.0f;
+    if (inter) {
+      o_szz[r] = szz[r] - (l2m[r] * dvz_dz + lam[r] * dvx_dx) * dt;
+      o_sxx[r] = sxx[r] - (lam[r] * dvz_dz + l2m[r] * dvx_dx) * dt;
+      e_own = dvx_dz + dvz_dx;
+      o_sxz[r] = sxz[r] - amu[r] * e_own * dt;
+      const float sa = s_szz_a[bb], xa = s_sxx_a[bb];
+      o_gl[r] = gl[r] + -(sa + xa) * (dvz_dz + dvx_dx) * dt * kMega;
+      gmu_own = (-2.0f * sa * dvz_dz * dt - 2.0f * xa * dvx_dx * dt) * kMega;
+    } else {
+      o_szz[r] = szz[r];
+      o_sxx[r] = sxx[r];
+      o_sxz[r] = sxz[r];
+      o_gl[r] = gl[r];
     }
-    if (hx[r] != 0.0f) {
-      const int bj = bb - BOXZ;
-      acc += w[r] * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, BOXZ, g.rdx)) * dt * hx[r]);
+    if constexpr (MID) {  // to_bnd of the stresses (the ring's values replace the update)
+      const int k = ring_index(g, zr, x);
+      if (k >= 0) {
+        const float* p = S.st.base + static_cast<size_t>(it) * 5 * g.ring_len + k;
+        o_szz[r] = p[0];
+        o_sxz[r] = p[g.ring_len];
+        o_sxx[r] = p[2 * g.ring_len];
+      }
     }
-    if (hzx != 0.0f) {
-      const int b2 = bb - BOXZ - 1;
-      acc += w[r] * (-s_sxz_a[b2] * (sdp(s_vx, b2, 1, g.rdz) + sdp(s_vz, b2, BOXZ, g.rdx)) * dt * hzx);
+    // mu kernel: own term and the three neighbouring 2x2 blocks; in a fast
+    // tile all guards hold, in a mid tile they are those of el_stress.cu:118-123.
+    if (!MID || in_box(zr, x, g.zi0, g.zi1, g.xi0, g.xi1 + 1)) {
+      const bool own_col = !MID || x <= g.xi1;
+      const bool up = !MID || zr - 1 >= g.zi0;
+      const bool left = !MID || x - 1 >= g.xi0;
+      float acc = gm[r] + gmu_own;
+      if (own_col) {
+        if (h[r] != 0.0f) acc += w[r] * (-s_sxz_a[bb] * e_own * dt * h[r]);
+        if (up && hz != 0.0f) {
+          const int bj = bb - 1;
+          acc += w[r] * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, BOXZ, g.rdx)) * dt * hz);
+        }
+      }
+      if (left) {
+        if (hx[r] != 0.0f) {
+          const int bj = bb - BOXZ;
+          acc += w[r] * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, BOXZ, g.rdx)) * dt * hx[r]);
+        }
+        if (up && own_col && hzx != 0.0f) {
+          const int b2 = bb - BOXZ - 1;
+          acc += w[r] * (-s_sxz_a[b2] * (sdp(s_vx, b2, 1, g.rdz) + sdp(s_vz, b2, BOXZ, g.rdx)) * dt * hzx);
+        }
+      }
+      o_gm[r] = acc;
+    } else {
+      o_gm[r] = gm[r];
     }
-    o_gm[r] = acc;
     // el_velocity_adj without the psi memory terms.
     {
       const float dszz_dx = -sdp(s_szz_a, bb, BOXZ, g.rdx);
@@ -988,7 +1064,12 @@ __device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int 
   str<R>(f.vz_a + i, o_vza);
 }
 
-template <int TX, int K, int R>
+// MID: a mid tile (no CPML cell): the adjoint memory arrays updated in their
+// bands (el_stress_adj.cu:68-94, within 2 cells of the CPML), the reverse
+// velocity update and its density terms only at cells of the reverse-time
+// interior, the ring's velocities of step it-1 restored, and the density
+// gathers with the guards of the edge form.
+template <int TX, int K, int R, bool MID>
 __device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int TZ = 32 * R, BOXZ = TZ + 8;
   SWEEP_FAST_SLOT(TZ)
@@ -1025,7 +1106,7 @@ __device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int 
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int bb = b + r;
-    if (special) {
+    if (special && z + r >= sh.rbz0 && z + r <= sh.rbz1) {
       const int2 rr = bin_range(sh, z + r, x);
       for (int k = rr.x; k < rr.y; ++k) {
         const int q = sh.blk_rec[k];
@@ -1047,6 +1128,20 @@ __device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int 
       xa[r] += bB[r] * dvx_dx * dt;
       sa[r] += bA[r] * dvz_dz * dt;
     }
+    if constexpr (MID) {
+      const int zr = z + r;
+      const bool xb = (x <= g.xband_lo) || (x >= g.xband_hi);
+      const bool zb = (zr <= g.zband_lo) || (zr >= g.zband_hi);
+      if (xb || zb) {
+        const CpmlD& c = S.c;
+        const size_t ir = i + r;
+        const float amu = m.aveMu[ir], lam = m.lam[ir], l2m = m.l2m[ir];
+        if (xb) f.m_dvz_dx[ir] = c.b_xh[x] * f.m_dvz_dx[ir] + za[r] * amu * dt;
+        if (zb) f.m_dvx_dz[ir] = c.b_zh[zr] * f.m_dvx_dz[ir] + za[r] * amu * dt;
+        if (xb) f.m_dvx_dx[ir] = c.b_x[x] * f.m_dvx_dx[ir] + lam * sa[r] * dt + l2m * xa[r] * dt;
+        if (zb) f.m_dvz_dz[ir] = c.b_z[zr] * f.m_dvz_dz[ir] + l2m * sa[r] * dt + lam * xa[r] * dt;
+      }
+    }
   }
   str<R>(f.sxz_a + i, za);
   str<R>(f.szz_a + i, sa);
@@ -1056,26 +1151,43 @@ __device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int 
   for (int r = 0; r < R; ++r) {
     const int bb = b + r;
     if (special && z + r == sh.src_z && x == sh.src_x) sh.gstf[it - 1] = -(sa[r] + 3.0f * xa[r]) * dt;
+    const int zr = z + r;
+    const bool inter = !MID || in_box(zr, x, g.zi0, g.zi1, g.xi0, g.xi1);
     const float ea = sdp(s_szz, bb, 1, g.rdz) + sdm(s_sxz, bb, BOXZ, g.rdx);  // dszz_dz + dsxz_dx
     const float eb = sdm(s_sxz, bb, 1, g.rdz) + sdp(s_sxx, bb, BOXZ, g.rdx);  // dsxz_dz + dsxx_dx
-    vz[r] = vz[r] - ea * bA[r] * dt;
-    vx[r] = vx[r] - eb * bB[r] * dt;
-    // rho kernel gather (all guards hold).
-    const float bAj = r == 0 ? bAj0 : bA[r - 1];  // bycA at (z-1, x)
-    float acc = gd[r];
-    acc += -s_vz_a[bb] * ea * dt * (-bA[r] * bA[r] * 0.5f);
-    acc += -s_vx_a[bb] * eb * dt * (-bB[r] * bB[r] * 0.5f);
-    {
-      const int bj = bb - 1;
-      const float e = sdp(s_szz, bj, 1, g.rdz) + sdm(s_sxz, bj, BOXZ, g.rdx);
-      acc += -s_vz_a[bj] * e * dt * (-bAj * bAj * 0.5f);
+    if (inter) {
+      vz[r] = vz[r] - ea * bA[r] * dt;
+      vx[r] = vx[r] - eb * bB[r] * dt;
     }
-    {
-      const int bj = bb - BOXZ;
-      const float e = sdm(s_sxz, bj, 1, g.rdz) + sdp(s_sxx, bj, BOXZ, g.rdx);
-      acc += -s_vx_a[bj] * e * dt * (-bBj[r] * bBj[r] * 0.5f);
+    if constexpr (MID) {  // to_bnd of the velocities of step it - 1
+      const int k = ring_index(g, zr, x);
+      if (k >= 0) {
+        const float* p = S.st.base + static_cast<size_t>(it - 1) * 5 * g.ring_len + k;
+        vz[r] = p[3 * g.ring_len];
+        vx[r] = p[4 * g.ring_len];
+      }
     }
-    gd[r] = acc;
+    // rho kernel gather: in a fast tile all guards hold, in a mid tile they
+    // are those of el_velocity.cu:101-110.
+    if (!MID || in_box(zr, x, g.zi0, g.zi1, g.xi0, g.xi1 + 1)) {
+      const float bAj = r == 0 ? bAj0 : bA[r - 1];  // bycA at (z-1, x)
+      float acc = gd[r];
+      if (!MID || x <= g.xi1) {
+        acc += -s_vz_a[bb] * ea * dt * (-bA[r] * bA[r] * 0.5f);
+        acc += -s_vx_a[bb] * eb * dt * (-bB[r] * bB[r] * 0.5f);
+        if (!MID || zr - 1 >= g.zi0) {
+          const int bj = bb - 1;
+          const float e = sdp(s_szz, bj, 1, g.rdz) + sdm(s_sxz, bj, BOXZ, g.rdx);
+          acc += -s_vz_a[bj] * e * dt * (-bAj * bAj * 0.5f);
+        }
+      }
+      if (!MID || x - 1 >= g.xi0) {
+        const int bj = bb - BOXZ;
+        const float e = sdm(s_sxz, bj, 1, g.rdz) + sdp(s_sxx, bj, BOXZ, g.rdx);
+        acc += -s_vx_a[bj] * e * dt * (-bBj[r] * bBj[r] * 0.5f);
+      }
+      gd[r] = acc;
+    }
   }
   str<R>(f.vz + i, vz);
   str<R>(f.vx + i, vx);
@@ -1235,7 +1347,7 @@ __device__ __forceinline__ void bwd_C_fast2(const SweepPack<K>& P, int shot, int
   const float2 XAm1 = ld2(s_vxa + b - B), XAp1 = ld2(s_vxa + b + B), XAm2 = ld2(s_vxa + b - 2 * B);
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
-    if (special) {
+    if (special && z + r >= sh.rbz0 && z + r <= sh.rbz1) {
       const int2 rr = bin_range(sh, z + r, x);
       for (int k = rr.x; k < rr.y; ++k) {
         const int q = sh.blk_rec[k];
@@ -1315,9 +1427,14 @@ __global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ SweepPack<K> P, 
   const bool inject = (flags & 2) != 0;
   if (fast) {
     if constexpr (R == 1)
-      fwd_stress_fast1<TX, K>(P, shot, z0, x0, it, inject, err);
+      fwd_stress_fast1<TX, K, false>(P, shot, z0, x0, it, 0, inject, err);
     else
-      fwd_stress_fast2<TX, K, R>(P, shot, z0, x0, it, inject, err);
+      fwd_stress_fast2<TX, K, R, false>(P, shot, z0, x0, it, 0, inject, err);
+  } else if (mid) {
+    if constexpr (R == 1)
+      fwd_stress_fast1<TX, K, true>(P, shot, z0, x0, it, flags & 1, inject, err);
+    else
+      fwd_stress_fast2<TX, K, R, true>(P, shot, z0, x0, it, flags & 1, inject, err);
   } else {
     fwd_stress_edge<TX, K, R>(P, shot, z0, x0, it, flags & 1, inject, err);
   }
@@ -1326,7 +1443,9 @@ __global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ SweepPack<K> P, 
 template <int TX, int K, int R>
 __global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ SweepPack<K> P, unsigned* err) {
   SWEEP_KERNEL_TILE(32 * R)
-  if (fast) {
+  // A mid tile of this sweep has nothing beyond the fast form: no CPML cell,
+  // every cell in the stencil domain, and no ring or band work.
+  if (fast || mid) {
     if constexpr (R == 1)
       fwd_velocity_fast1<TX, K>(P, shot, z0, x0, err);
     else
@@ -1342,9 +1461,11 @@ __global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ SweepPack<K> P, int j
   SWEEP_KERNEL_TILE(32 * R)
   if (fast) {
     if constexpr (R == 1)
-      bwd_B_fast<TX, K, 1>(P, shot, z0, x0, j, err);
+      bwd_B_fast<TX, K, 1, false>(P, shot, z0, x0, j, err);
     else
       bwd_B_fast2<TX, K>(P, shot, z0, x0, j, err);
+  } else if (mid) {
+    bwd_B_fast<TX, K, R, true>(P, shot, z0, x0, j, err);
   } else {
     bwd_B_edge<TX, K, R>(P, shot, z0, x0, j, err);
   }
@@ -1355,9 +1476,11 @@ __global__ void BWD_BOUNDS k_bwd_C(const __grid_constant__ SweepPack<K> P, int j
   SWEEP_KERNEL_TILE(32 * R)
   if (fast) {
     if constexpr (R == 1)
-      bwd_C_fast<TX, K, 1>(P, shot, z0, x0, j, err);
+      bwd_C_fast<TX, K, 1, false>(P, shot, z0, x0, j, err);
     else
       bwd_C_fast2<TX, K>(P, shot, z0, x0, j, err);
+  } else if (mid) {
+    bwd_C_fast<TX, K, R, true>(P, shot, z0, x0, j, err);
   } else {
     bwd_C_edge<TX, K, R>(P, shot, z0, x0, j, err);
   }
