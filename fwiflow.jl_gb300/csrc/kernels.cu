@@ -31,10 +31,15 @@ constexpr float C1 = 1.125f;          // 9/8  (el_stress.cu:42)
 constexpr float C2 = 1.0f / 24.0f;    // 1/24 (el_stress.cu:43)
 constexpr float kMega = 1.0e6f;       // MEGA (utilities.h:16)
 
-// Bounded waits: a sweep that waits this many polls for its staged tiles
-// gives up, raises its error word and returns instead of hanging.
-constexpr unsigned kSpinLimit = 1u << 22;
-// Polls of the injected wait of the timeout test hook (stage_wait).
+// Bounded waits: a sweep that has waited this long (global timer) for its
+// staged tiles gives up, raises its error word and returns instead of
+// hanging. Each poll asks the hardware to suspend the thread until the
+// barrier phase completes or kWaitHintNs pass, so a waiting warp issues a
+// few instructions instead of spinning.
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;
+constexpr unsigned kWaitHintNs = 1000000u;
+// Polls (without a suspend hint) of the injected wait of the timeout test
+// hook (stage_wait).
 constexpr unsigned kInjectPolls = 256;
 
 // ---- mbarrier / TMA (sm_90+ PTX; issued by one thread per block) ----
@@ -57,8 +62,32 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, unsigned limit = kSpinLimit) {
-  for (unsigned n = 0; n < limit; ++n)
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(kWaitHintNs)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_timer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Waits for phase `parity` of the barrier, at most kWaitLimitNs.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+  if (mbar_try_wait_hint(bar, parity)) return true;
+  const unsigned long long t0 = global_timer_ns();
+  for (;;) {
+    if (mbar_try_wait_hint(bar, parity)) return true;
+    if (global_timer_ns() - t0 > kWaitLimitNs) return false;
+  }
+}
+// Polls phase `parity` of the barrier `polls` times without a suspend hint.
+__device__ __forceinline__ bool mbar_poll(uint64_t* bar, unsigned parity, unsigned polls) {
+  for (unsigned n = 0; n < polls; ++n)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -113,7 +142,7 @@ __device__ __forceinline__ bool stage_wait(uint64_t* bar, unsigned* err, bool in
     mbar_wait_bounded(bar, 0);
     return false;
   }
-  if (inject && !mbar_wait_bounded(bar, 1, kInjectPolls)) {
+  if (inject && !mbar_poll(bar, 1, kInjectPolls)) {
     atomicOr(err, 1u);
     return false;
   }
