@@ -15,10 +15,18 @@ error, learned vs plain, on one GPU.
    (lbfgs_pseudo_hessian) gain; each records misfit, model error and wall
    time per iteration.
 
-    python fwiflow.jl_gb300/learned_fwi.py [--train-models 64] [--eval-models 4] [--iters 20] [--out FILE]
+4. Extended runs (--long-models M --long-iters N): on the first M held-out
+   models, plain L-BFGS and learned L-BFGS continue to N iterations; each
+   records its lowest relative model error, the time to reach it, and the
+   time to the target error if it gets there.
+
+    python fwiflow.jl_gb300/learned_fwi.py [--train-models 64] [--eval-models 4] [--iters 20]
+                                           [--long-models 0] [--long-iters 100] [--out FILE]
 
 prints one JSON line (per method: the median over the held-out models of the
-time to the target error and of the final error).
+time to the target error and of the final error; the learned methods also
+with the training cost -- data generation plus training -- spread over the
+held-out inversions, and added in full).
 """
 from __future__ import annotations
 
@@ -55,6 +63,8 @@ def main(argv=None) -> None:
     ap.add_argument("--train-seed", type=int, default=1000)
     ap.add_argument("--eval-seed", type=int, default=2000)
     ap.add_argument("--methods", default="plain,learned,pseudo_hessian,lbfgs")
+    ap.add_argument("--long-models", type=int, default=0, help="held-out models of the extended runs")
+    ap.add_argument("--long-iters", type=int, default=100, help="iterations of the extended runs")
     ap.add_argument("--out", default=None, help="write the full histories (JSON) here")
     args = ap.parse_args(argv)
 
@@ -133,25 +143,60 @@ def main(argv=None) -> None:
         v = [x for x in v if x is not None]
         return float(np.median(v)) if v else None
 
+    # Extended runs: does either L-BFGS reach the target, and how low does it go?
+    long_runs = {"lbfgs": [], "lbfgs_learned": []}
+    for w in evals[:args.long_models]:
+        for m in long_runs:
+            prob = problem_of(w)
+            gain = inversion.learned_gain(net) if m == "lbfgs_learned" else None
+            h = inversion.lbfgs(prob, args.long_iters, gain=gain)
+            k = int(np.argmin(h.model_error))
+            long_runs[m].append({"seed": w.extra["seed"], "iters": len(h.model_error) - 1,
+                                 "start_error": h.model_error[0], "lowest_error": h.model_error[k],
+                                 "iteration_of_lowest": k, "time_to_lowest_s": h.wall[k],
+                                 "time_to_target_s": h.time_to_error(args.target_error),
+                                 "final_misfit_ratio": h.misfit[-1] / h.misfit[0], "wall_s": h.wall[-1],
+                                 "history": h.as_dict()})
+            log(f"extended model {w.extra['seed']} {m:15s} lowest error {h.model_error[k]:.5f} at it {k} "
+                f"({h.wall[k]:.1f} s); time to {args.target_error:g}: {h.time_to_error(args.target_error)}")
+
+    train_cost = t_data + t_train
+    n_inv = max(1, len(evals))
     summary = {}
     for m, rs in results.items():
         tt = [r["time_to_target_s"] for r in rs]
+        tp = [r["time_to_plain_final_s"] for r in rs]
         summary[m] = {"reached": sum(t is not None for t in tt), "models": len(rs),
                       "median_time_to_target_s": med(tt),
-                      "median_time_to_plain_final_error_s": med([r["time_to_plain_final_s"] for r in rs]),
+                      "median_time_to_plain_final_error_s": med(tp),
                       "median_final_misfit_ratio": med([r["misfit"][-1] / r["misfit"][0] for r in rs]),
                       "median_final_error": med([r["model_error"][-1] for r in rs]),
                       "median_start_error": med([r["model_error"][0] for r in rs]),
                       "median_wall_s": med([r["wall_s"][-1] for r in rs])}
+        if "learned" in m:  # the network's cost: amortised over the held-out inversions, and in full
+            summary[m]["median_time_to_plain_final_error_with_amortised_training_s"] = med(
+                [None if t is None else t + train_cost / n_inv for t in tp])
+            summary[m]["median_time_to_plain_final_error_with_full_training_s"] = med(
+                [None if t is None else t + train_cost for t in tp])
+    extended = {}
+    for m, rs in long_runs.items():
+        if rs:
+            extended[m] = {"models": len(rs), "iters": args.long_iters,
+                           "reached_target": sum(r["time_to_target_s"] is not None for r in rs),
+                           "median_lowest_error": med([r["lowest_error"] for r in rs]),
+                           "median_time_to_lowest_s": med([r["time_to_lowest_s"] for r in rs]),
+                           "median_start_error": med([r["start_error"] for r in rs]),
+                           "per_model": [{k: v for k, v in r.items() if k != "history"} for r in rs]}
     line = {"experiment": "time to relative model error, learned vs plain preconditioner",
             "target_error": args.target_error, "grid": [w0.nz_pad, w0.nx_pad], "nSteps": args.nsteps,
             "shots": args.shots, "train_models": args.train_models, "eval_models": args.eval_models,
             "iters": args.iters, "training_data_s": t_data, "training_s": t_train, "train_loss": hist,
-            "heldout_loss": [loss0, val_loss], "methods": summary}
+            "heldout_loss": [loss0, val_loss], "methods": summary, "extended_runs": extended}
     print(json.dumps(line))
     if args.out:
         with open(args.out, "w") as f:
-            json.dump({"summary": line, "histories": results}, f)
+            json.dump({"summary": line, "histories": results,
+                   "extended_histories": {m: [r["history"] for r in rs] for m, rs in long_runs.items()}}, f)
     ctx.close()
 
 
