@@ -78,21 +78,21 @@ def workload(name, nsteps=None, shots=None):
     return synthetic.dipping_grf(**({"nSteps": nsteps} if nsteps else {}))
 
 
-def shot_sizes(w):
-    """(cells, steps) of every shot: its sub-grid (aperture window + 2 nPml
-    columns) and its record length."""
+def shot_sizes(w, ids=None):
+    """(cells, steps) of every shot (or of the shots `ids`): its sub-grid
+    (aperture window + 2 nPml columns) and its record length."""
     out = []
-    for s in w.shots:
+    for s in (w.shots if ids is None else [w.shots[k] for k in ids]):
         nx = s["win_x1"] - s["win_x0"] + 1 + 2 * w.nPml if "win_x0" in s else w.nx_pad
         out.append((w.nz_pad * nx, int(s.get("nSteps", w.nSteps))))
     return out
 
 
-def sweep_cell_steps(w):
-    """Cell-steps each sweep kind processes in one misfit + gradient call:
-    forward stress / velocity and backward B run nSteps-1 times per shot,
-    backward C nSteps times."""
-    sz = shot_sizes(w)
+def sweep_cell_steps(w, ids=None):
+    """Cell-steps each sweep kind processes in one misfit + gradient call
+    (over the shots `ids`, default all): forward stress / velocity and
+    backward B run nSteps-1 times per shot, backward C nSteps times."""
+    sz = shot_sizes(w, ids)
     fwd = sum(c * (n - 1) for c, n in sz)
     return [fwd, fwd, fwd, sum(c * n for c, n in sz)]
 
@@ -244,12 +244,27 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    w = workload(args.workload, args.nsteps, args.shots)
+    # With N > 1 ranks the multi-shot workloads grow to N times their shots
+    # (the first shots are those of the one-rank workload) and every rank
+    # takes its cost-balanced share (weak scaling, no exchange in the timed
+    # region); a lone-shot workload runs as N replicas.
+    sharded = world > 1 and args.workload in ("batched_uneven", "faulted_grf")
+    default_shots = {"batched_uneven": 64, "faulted_grf": 16}.get(args.workload)
+    w = workload(args.workload, args.nsteps, (args.shots or default_shots) * world if sharded else args.shots)
     metric, unit = "fwd+adj Gpts/s vs HBM roofline", "Gpts/s"
-    cell_steps = sum(c * n for c, n in shot_sizes(w))
+    all_ids = list(range(len(w.shots)))
+    if sharded:
+        from fwiflow_gb300.shots import shard_shots, shot_costs
+
+        costs = shot_costs(shot_sizes(w))
+        ids = shard_shots(all_ids, world, costs)[rank]
+    else:
+        costs, ids = None, all_ids
+    cell_steps = sum(c * n for c, n in shot_sizes(w))  # whole job (all ranks' shots when sharded)
     cfg = {"workload": describe(w), "cells": w.cells, "nSteps": w.nSteps, "shots": len(w.shots),
            "cell_steps_per_call": cell_steps,
-           "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+           "parallelism": (f"shots sharded over {world} ranks" if sharded else f"replicas x{world}") if world > 1
+           else "single GPU",
            "l2": "flushed between timed steps (256 MiB write); each step also streams a "
                  f"{store_gib(w):.2f} GiB boundary store"}
 
@@ -294,7 +309,6 @@ def main():
         ctx.set_tile_config([int(v) for v in args.tile_widths.split(",")])
     if args.tile_rows:
         ctx.set_tile_rows([int(v) for v in args.tile_rows.split(",")])
-    ids = list(range(len(w.shots)))
     obs = ctx.obs(*w.moduli(w.vp_obs), w.stf, ids, write_files=False)
     lam, mu, rho = w.moduli()
     ctx.set_model(lam, mu, rho)
@@ -340,8 +354,9 @@ def main():
         t = torch.tensor([dev_s, wall], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         dev_s, wall = float(t[0]), float(t[1])
-    pts_step = cell_steps
-    value = world * pts_step * args.steps / dev_s / 1e9
+    pts_step = sum(c * n for c, n in shot_sizes(w, ids))  # this rank's cell-steps per call
+    job_pts = cell_steps if sharded else world * pts_step
+    value = job_pts * args.steps / dev_s / 1e9
 
     # Per-sweep timing for the roofline, measured inside one call: an event
     # pair around every sweep step (all shot packs of the step; the pair costs
@@ -356,7 +371,7 @@ def main():
     # Supplementary: a CUDA graph of 50 back-to-back sweep steps over the
     # whole group (no event pair between them).
     us_graph = np.array([ctx.sweep_time(k, 50) for k in range(4)])
-    cs = sweep_cell_steps(w)
+    cs = sweep_cell_steps(w, ids)
     k_dom = int(np.argmax(tot_ms))
     peak, peak_kind = peaks()
     kbytes_call = [SWEEP_BYTES[k] * cs[k] for k in range(4)]
@@ -398,11 +413,22 @@ def main():
 
     ids_a = np.asarray(ids, dtype=np.int32)
 
-    def e2e_call():
+    def rank_call(l, m, d, stf, mine):
+        assert list(mine) == list(ids)
         _lib.check(lib.fwigb_misfit_grad_obs(ctx._h, _lib.dptr(lam_h), _lib.dptr(mu_h), _lib.dptr(rho_h),
                                              _lib.dptr(stf_h), stf_h.shape[0], _lib.iptr(ids_a), len(ids),
                                              _lib.fptr(obs_h), _lib.dptr(mis), _lib.dptr(out["gl"]),
                                              _lib.dptr(out["gm"]), _lib.dptr(out["gd"]), _lib.dptr(gs_h)), ctx._h)
+        return float(mis[0]), out["gl"], out["gm"], out["gd"], gs_h
+
+    def e2e_call():
+        if sharded:  # a data-parallel step: this rank's shots, then one all-reduce of misfit and gradients
+            from fwiflow_gb300.shots import sharded_misfit_grad
+
+            sharded_misfit_grad(rank_call, lam_h, mu_h, rho_h, stf_h, all_ids, rank=rank, world=world, costs=costs,
+                                device=torch.device("cuda", local_rank))
+        else:
+            rank_call(lam_h, mu_h, rho_h, stf_h, ids)
 
     e2e_call()
     n_e2e = max(1, min(args.steps, args.e2e_steps))
@@ -416,7 +442,7 @@ def main():
         t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t[0])
-    e2e_val = world * pts_step * n_e2e / e2e_s / 1e9
+    e2e_val = job_pts * n_e2e / e2e_s / 1e9
     h2d = 3 * w.cells * 8 + stf_h.nbytes + obs_h.nbytes
     d2h = 3 * w.cells * 8 + len(ids) * w.nSteps * 8 + 8
 
@@ -439,7 +465,8 @@ def main():
         s_single = e0.elapsed_time(e1) / 1e3
         ctx.set_batching(max_shots=0)
         single = {"value": pts_step / s_single / 1e9, "unit": unit, "ms_per_step": 1e3 * s_single,
-                  "groups": ctx.last_group_count(), "batched_over_single": value / (pts_step / s_single / 1e9),
+                  "groups": ctx.last_group_count(),
+                  "batched_over_single": (pts_step * args.steps / dev_s) / (pts_step / s_single),
                   "note": "same call, every shot in a group of its own (one shot per launch)"}
 
     if rank != 0:
