@@ -21,10 +21,13 @@
 //                  transposed kernel: dX = conv(dZ, W'))
 //   k_conv3x3_wgrad  per-block partial dW[tap][ci][co] = sum_p X(p+tap) dZ(p)
 //   k_reduce_partials, k_bias_grad, k_adam, k_pack_weights, k_mse_grad
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "fwiflow_gb300.h"
 
@@ -176,13 +179,37 @@ __global__ void __launch_bounds__(256) k_conv3x3(const __nv_bfloat16* __restrict
 // channels, 8-row core matrices 128 bytes apart (SBO) and channel groups LBO
 // apart. Rows of the input tile are consecutive depths of one column, so the
 // operand of a tap (ky, kx) is the tile column x + kx started ky rows down: a
-// descriptor offset of 16 ky bytes. One thread issues the MMAs; the FP32
-// accumulators (4 columns x 32 couts = 128 TMEM columns) are read back by
-// the block's two warpgroups with tcgen05.ld (warp w owns TMEM lanes
-// 32 (w % 4) .. +31, i.e. depths z0 + 32 (w % 4) + lane; warpgroup g takes
-// columns 2g and 2g + 1) and go through the fused epilogue.
-constexpr int kTcRows = 128, kTcCols = 4;  // pixels per block: 128 depths x 4 columns
+// descriptor offset of 16 ky bytes.
+//
+// Persistent and warp-specialised: one CTA per SM walks the image's tiles
+// (128 depths x 4 columns each) with a stride of the grid.
+//   warp 0 (one thread)  TMA producer: the input tile with its 1-pixel halo,
+//                        130 depths x 6 columns x CIN channels, as CIN/8 3-D
+//                        boxes (8 channels x 130 x 6, zero fill outside the
+//                        image) into a kTcStages-deep ring of shared-memory
+//                        stages; a box lands exactly in the K-major layout
+//                        above (16-byte units, depth fastest, then column).
+//   warp 1 (one thread)  MMA issuer: 4 columns x 9 taps x CIN/16 tcgen05.mma
+//                        per tile into one of kTcAcc tensor-memory
+//                        accumulators (4 columns x 32 couts = 128 TMEM
+//                        columns each); tcgen05.commit frees the stage and
+//                        publishes the accumulator.
+//   warps 4..19          epilogue: warpgroup g reads column g of the
+//                        accumulator with tcgen05.ld (warp w owns TMEM lanes
+//                        32 (w % 4) .. +31, i.e. depths z0 + 32 (w % 4) +
+//                        lane), applies the fused epilogue and stores BF16,
+//                        then releases the accumulator.
+// So the load of tile i+1, the MMAs of tile i+1 and the epilogue of tile i
+// overlap. The weights (B operand) are loaded once per CTA. Every wait is
+// bounded by the global timer: a role whose wait runs out raises bit 1 of
+// *err and stops; the others then run out too, and the CTA frees its tensor
+// memory and returns.
+constexpr int kTcRows = 128, kTcCols = 4;  // pixels per tile: 128 depths x 4 columns
 constexpr int kTcTileRows = kTcRows + 2, kTcTileCols = kTcCols + 2;
+constexpr int kTcStages = 2, kTcAcc = 2;
+constexpr int kTcThreads = 640;  // warps 0..3: producer, MMA, 2 idle; warps 4..19: 4 epilogue warpgroups
+constexpr uint32_t kTcBox = kTcTileRows * kTcTileCols * 16;  // bytes of one 8-channel box
+constexpr uint32_t kTcBoxStride = (kTcBox + 127) / 128 * 128;  // boxes 128-byte aligned in a stage
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -190,29 +217,46 @@ __device__ __forceinline__ unsigned long long global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-__device__ __forceinline__ void mbar_init1(uint64_t* bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+__device__ __forceinline__ void mbar_init_n(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 __device__ __forceinline__ bool mbar_test(uint64_t* bar, unsigned parity) {
   unsigned ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(1000000u)
       : "memory");
   return ok != 0;
 }
 // Bounded wait (global timer) for phase `parity` of an mbarrier.
 __device__ __forceinline__ bool mbar_wait_ns(uint64_t* bar, unsigned parity) {
+  if (mbar_test(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
-  for (unsigned n = 0;; ++n) {
+  for (;;) {
     if (mbar_test(bar, parity)) return true;
-    if ((n & 255u) == 255u && global_ns() - t0 > kTcWaitNs) return false;
+    if (global_ns() - t0 > kTcWaitNs) return false;
   }
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, int c0, int c1, int c2, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
 
 // Shared-memory matrix descriptor: start, leading (K-direction) and stride
 // (8-row-group) byte offsets, all >> 4; descriptor version 1; no swizzle.
@@ -249,79 +293,119 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
 
 // CIN in {16, 32} input channels, 32 output channels. EPI kEpiGelu (bias,
 // pre-activation and GELU, BF16) or kEpiDGelu (times GELU'(z_prev), BF16).
-// wpack: the B operand in its shared-memory layout, 16-byte units (q, n) at
-// (q * 32 + n) for q = tap * CIN/8 + channel group (k_pack_weights_tc).
+// tmap: the input image as a 3-D tensor (channels, depths, columns), box
+// 8 x 130 x 6. wpack: the B operand in its shared-memory layout, 16-byte
+// units (q, n) at (q * 32 + n) for q = tap * CIN/8 + channel group
+// (k_pack_weights_tc).
 template <int CIN, int EPI>
-__global__ void __launch_bounds__(256) k_conv3x3_tc(const __nv_bfloat16* __restrict__ x_in, int Hz, int Wx,
-                                                    const uint4* __restrict__ wpack,
-                                                    const float* __restrict__ bias, __nv_bfloat16* __restrict__ y,
-                                                    __nv_bfloat16* __restrict__ z_pre,
-                                                    const __nv_bfloat16* __restrict__ z_prev, unsigned* err) {
-  constexpr int QA = CIN / 8;                                    // channel groups of the input
-  constexpr int A_UNITS = QA * kTcTileCols * kTcTileRows;        // 16-byte units of the input tile
-  constexpr uint32_t LBO_A = kTcTileCols * kTcTileRows * 16;     // between channel groups
-  constexpr int QB = 9 * CIN / 8;                                // channel groups of B over the taps
-  constexpr uint32_t A_BYTES = A_UNITS * 16;
-  extern __shared__ __align__(128) uint8_t tc_smem[];
-  uint4* sA = reinterpret_cast<uint4*>(tc_smem);
-  uint4* sB = reinterpret_cast<uint4*>(tc_smem + A_BYTES);
-  __shared__ __align__(8) uint64_t mbar;
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_conv3x3_tc(const __grid_constant__ CUtensorMap tmap, int Hz, int Wx, const uint4* __restrict__ wpack,
+                 const float* __restrict__ bias, __nv_bfloat16* __restrict__ y, __nv_bfloat16* __restrict__ z_pre,
+                 const __nv_bfloat16* __restrict__ z_prev, unsigned* err) {
+  constexpr int QA = CIN / 8;                    // channel groups (boxes) of the input
+  constexpr uint32_t STAGE = QA * kTcBoxStride;  // bytes of one input stage
+  constexpr int QB = 9 * CIN / 8;                // channel groups of B over the taps
+  extern __shared__ __align__(1024) uint8_t tc_smem[];
+  uint8_t* sA = tc_smem;                            // kTcStages stages
+  uint4* sB = reinterpret_cast<uint4*>(tc_smem + kTcStages * STAGE);
+  __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages], acc_full[kTcAcc], acc_empty[kTcAcc];
   __shared__ uint32_t tmem_slot;
-  const int z0 = blockIdx.x * kTcRows, x0 = blockIdx.y * kTcCols;
+  __shared__ int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ntz = (Hz + kTcRows - 1) / kTcRows, ntx = (Wx + kTcCols - 1) / kTcCols, ntiles = ntz * ntx;
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(&tmem_slot))
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kTcAcc * 128)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  for (int u = tid; u < A_UNITS; u += blockDim.x) {
-    const int q = u % QA, rest = u / QA;
-    const int r = rest % kTcTileRows, c = rest / kTcTileRows;
-    const int z = z0 + r - 1, x = x0 + c - 1;
-    uint4 v = make_uint4(0u, 0u, 0u, 0u);
-    if (z >= 0 && z < Hz && x >= 0 && x < Wx)
-      v = *reinterpret_cast<const uint4*>(x_in + (static_cast<size_t>(x) * Hz + z) * CIN + q * 8);
-    sA[(q * kTcTileCols + c) * kTcTileRows + r] = v;
-  }
   for (int u = tid; u < QB * 32; u += blockDim.x) sB[u] = wpack[u];
-  if (tid == 0) mbar_init1(&mbar);
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // operands visible to the tensor cores
+  if (tid == 0) {
+    for (int k = 0; k < kTcStages; ++k) {
+      mbar_init_n(&full[k], 1);
+      mbar_init_n(&empty[k], 1);
+    }
+    for (int k = 0; k < kTcAcc; ++k) {
+      mbar_init_n(&acc_full[k], 1);
+      mbar_init_n(&acc_empty[k], 16 * 32);  // every epilogue thread
+    }
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // weights visible to the tensor cores
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
-  if (tid == 0) {
-    const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-#pragma unroll 1
-    for (int j = 0; j < kTcCols; ++j)
-#pragma unroll 1
-      for (int tap = 0; tap < 9; ++tap) {
-        const int ky = tap / 3, kx = tap % 3;
-#pragma unroll
-        for (int s = 0; s < CIN / 16; ++s) {
-          const uint32_t a = a0 + ((2 * s * kTcTileCols + (j + kx)) * kTcTileRows + ky) * 16;
-          const uint32_t b = b0 + (tap * QA + 2 * s) * 32 * 16;
-          tc_mma(tmem + j * 32, smem_desc(a, LBO_A, 128), smem_desc(b, 32 * 16, 128), (tap | s) != 0);
+  if (warp == 0) {
+    if (lane == 0) {  // TMA producer
+      int i = 0;
+      for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+        const int st = i % kTcStages;
+        if (i >= kTcStages && !mbar_wait_ns(&empty[st], ((i / kTcStages) - 1) & 1)) {
+          atomicOr(err, 2u);
+          atomicExch(&abort_flag, 1);
+          break;
         }
+        if (*reinterpret_cast<volatile int*>(&abort_flag)) break;
+        const int z0 = (t % ntz) * kTcRows, x0 = (t / ntz) * kTcCols;
+        mbar_expect_tx(&full[st], QA * kTcBox);
+#pragma unroll
+        for (int q = 0; q < QA; ++q) tma_load_3d(sA + st * STAGE + q * kTcBoxStride, &tmap, q * 8, z0 - 1, x0 - 1, &full[st]);
       }
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                     smem_u32(&mbar))
-                 : "memory");
-  }
-  bool ok = mbar_wait_ns(&mbar, 0);
-  if (!ok) {
-    atomicOr(err, 2u);
-    mbar_wait_ns(&mbar, 0);  // let MMAs in flight finish before the memory goes away
-  }
-  ok = __all_sync(0xffffffffu, ok);
-  tc_fence_after();
-  if (ok) {
-    const int quarter = warp & 3, wg = warp >> 2;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      const uint32_t b0 = smem_u32(sB);
+      int i = 0;
+      for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+        const int st = i % kTcStages, ac = i % kTcAcc;
+        bool ok = mbar_wait_ns(&full[st], (i / kTcStages) & 1);
+        if (ok && i >= kTcAcc) ok = mbar_wait_ns(&acc_empty[ac], ((i / kTcAcc) - 1) & 1);
+        if (!ok || *reinterpret_cast<volatile int*>(&abort_flag)) {
+          atomicOr(err, 2u);
+          atomicExch(&abort_flag, 1);
+          break;
+        }
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(sA + st * STAGE);
+        const uint32_t d0 = tmem + ac * 128;
 #pragma unroll 1
-    for (int j = 2 * wg; j < 2 * wg + 2; ++j) {
+        for (int j = 0; j < kTcCols; ++j)
+#pragma unroll 1
+          for (int tap = 0; tap < 9; ++tap) {
+            const int ky = tap / 3, kx = tap % 3;
+#pragma unroll
+            for (int s = 0; s < CIN / 16; ++s) {
+              const uint32_t a = a0 + 2 * s * kTcBoxStride + ((j + kx) * kTcTileRows + ky) * 16;
+              const uint32_t b = b0 + (tap * QA + 2 * s) * 32 * 16;
+              tc_mma(d0 + j * 32, smem_desc(a, kTcBoxStride, 128), smem_desc(b, 32 * 16, 128), (tap | s) != 0);
+            }
+          }
+        tc_commit(&empty[st]);    // the stage is free once these MMAs have read it
+        tc_commit(&acc_full[ac]);  // and the accumulator is ready
+      }
+    }
+  } else if (warp >= 4) {  // epilogue: warpgroup g takes pixel column g of each tile
+    const int g = (warp - 4) >> 2, quarter = warp & 3;
+    int i = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+      const int ac = i % kTcAcc;
+      const bool ok = __all_sync(0xffffffffu, mbar_wait_ns(&acc_full[ac], (i / kTcAcc) & 1));
+      if (!ok) {
+        if (lane == 0) {
+          atomicOr(err, 2u);
+          atomicExch(&abort_flag, 1);
+        }
+        break;
+      }
+      tc_fence_after();
+      const int z0 = (t % ntz) * kTcRows, x0 = (t / ntz) * kTcCols;
       float v[32];
-      tc_ld32(tmem + (static_cast<uint32_t>(quarter * 32) << 16) + j * 32, v);
-      const int z = z0 + quarter * 32 + lane, x = x0 + j;
+      tc_ld32(tmem + (static_cast<uint32_t>(quarter * 32) << 16) + ac * 128 + g * 32, v);
+      tc_fence_before();
+      mbar_arrive(&acc_empty[ac]);  // the accumulator's column is in registers
+      const int z = z0 + quarter * 32 + lane, x = x0 + g;
       if (z < Hz && x < Wx) {
         const size_t p = (static_cast<size_t>(x) * Hz + z) * 32;
         unsigned o0[16], o1[16];
@@ -358,9 +442,14 @@ __global__ void __launch_bounds__(256) k_conv3x3_tc(const __nv_bfloat16* __restr
       }
     }
   }
+  // Teardown: the epilogue has taken every accumulator the MMA thread
+  // committed (or the CTA aborted on a timeout, after each role's own bounded
+  // wait), so the tensor memory is free to go.
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
+  tc_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcAcc * 128)
+                              : "memory");
 }
 
 // Packs W[9][cin][cout] (FP32) into the B operand of k_conv3x3_tc: unit
@@ -584,6 +673,31 @@ cudaError_t conv(const void* x, int Hz, int Wx, const void* wfrag, const float* 
   return cudaGetLastError();
 }
 
+// The input image of k_conv3x3_tc as a 3-D tensor map: dimensions (cin
+// channels, Hz depths, Wx columns) of BF16, box 8 x 130 x 6, zero fill
+// outside. cuTensorMapEncodeTiled checks the base (16-byte aligned) and the
+// strides (cin * 2 and Hz * cin * 2 bytes, multiples of 16); every copy's
+// channel coordinate is a multiple of 8 (16 bytes).
+bool encode_input_map(CUtensorMap* m, const void* x, int Hz, int Wx, int cin) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  });
+  if (!encode || reinterpret_cast<uintptr_t>(x) % 16 != 0) return false;
+  const cuuint64_t dims[3] = {static_cast<cuuint64_t>(cin), static_cast<cuuint64_t>(Hz), static_cast<cuuint64_t>(Wx)};
+  const cuuint64_t strides[2] = {static_cast<cuuint64_t>(cin) * 2, static_cast<cuuint64_t>(Hz) * cin * 2};
+  const cuuint32_t box[3] = {8, static_cast<cuuint32_t>(kTcTileRows), static_cast<cuuint32_t>(kTcTileCols)};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(x), dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 }  // namespace
 }  // namespace fwigb_cnn
 
@@ -648,27 +762,31 @@ int fwigb_cnn_conv3x3_tc(const void* x, int Hz, int Wx, int cin_pad, int epilogu
   if (epilogue == kEpiGelu && (!bias || !z_pre)) return FWIGB_ERR_ARG;
   if (epilogue == kEpiDGelu && !z_prev) return FWIGB_ERR_ARG;
   if (epilogue != kEpiGelu && epilogue != kEpiDGelu) return FWIGB_ERR_UNSUPPORTED;
+  if (cin_pad != 16 && cin_pad != 32) return FWIGB_ERR_UNSUPPORTED;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const dim3 grid((Hz + kTcRows - 1) / kTcRows, (Wx + kTcCols - 1) / kTcCols);
-  const auto* xi = static_cast<const __nv_bfloat16*>(x);
+  CUtensorMap tmap;
+  if (!encode_input_map(&tmap, x, Hz, Wx, cin_pad)) return FWIGB_ERR_CUDA;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return FWIGB_ERR_CUDA;
+  const int ntiles = ((Hz + kTcRows - 1) / kTcRows) * ((Wx + kTcCols - 1) / kTcCols);
+  const int grid = ntiles < sms ? ntiles : sms;  // persistent: at most one CTA per SM
   const auto* wp = static_cast<const uint4*>(wpack);
   auto* yo = static_cast<__nv_bfloat16*>(y_bf16);
   auto* zo = static_cast<__nv_bfloat16*>(z_pre);
   const auto* zi = static_cast<const __nv_bfloat16*>(z_prev);
   auto launch = [&](auto kernel, int cin) -> cudaError_t {
-    const size_t smem = static_cast<size_t>(cin / 8) * kTcTileCols * kTcTileRows * 16 + 9 * cin / 8 * 32 * 16;
+    const size_t smem = static_cast<size_t>(kTcStages) * (cin / 8) * kTcBoxStride + 9 * cin / 8 * 32 * 16;
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    kernel<<<grid, 256, smem, s>>>(xi, Hz, Wx, wp, bias, yo, zo, zi, err_word);
+    kernel<<<grid, kTcThreads, smem, s>>>(tmap, Hz, Wx, wp, bias, yo, zo, zi, err_word);
     return cudaGetLastError();
   };
   cudaError_t e;
   if (cin_pad == 16)
     e = epilogue == kEpiGelu ? launch(k_conv3x3_tc<16, kEpiGelu>, 16) : launch(k_conv3x3_tc<16, kEpiDGelu>, 16);
-  else if (cin_pad == 32)
-    e = epilogue == kEpiGelu ? launch(k_conv3x3_tc<32, kEpiGelu>, 32) : launch(k_conv3x3_tc<32, kEpiDGelu>, 32);
   else
-    return FWIGB_ERR_UNSUPPORTED;
+    e = epilogue == kEpiGelu ? launch(k_conv3x3_tc<32, kEpiGelu>, 32) : launch(k_conv3x3_tc<32, kEpiDGelu>, 32);
   return e == cudaSuccess ? FWIGB_OK : FWIGB_ERR_CUDA;
 }
 

@@ -1,6 +1,7 @@
 """Batched shots on the sm_103a path: shots with their own aperture window and
 record length, run as concurrent groups (one launch per sweep and time step
-for up to 16 shots, more launches for larger groups).
+covers every active shot of the group, which reads its slot and tensor maps
+from a device table; a one-group call replays from a CUDA graph).
 
 A windowed shot is defined as the reference run alone on the shot's sub-model
 (padded columns win_x0 .. win_x1 + 2 nPml) for its own record length, its
@@ -164,4 +165,36 @@ def test_illumination_matches_oracle(gpu_lib, fw, orc, tmp_path):
     assert ctx.misfit(lam, mu, rho, w.stf, ids) == pytest.approx(J, rel=1e-6)
     with pytest.raises(fw.FwiError):
         ctx.illumination()
+    ctx.close()
+
+
+def test_batched_graph_replay_is_identical(gpu_lib, fw, orc, tmp_path):
+    """A batched group (one launch per sweep step for all its shots, reading
+    their slots and tensor maps from a device table) replays its whole call
+    from a CUDA graph: same bits as eager launches, across a model change
+    (replay) and a different shot set (re-recorded); and the replayed call
+    matches the oracle."""
+    w = uneven_tiny(n_shots=6, seed=17)
+    para = w.write_files(str(tmp_path))
+    ids = list(range(len(w.shots)))
+    ref = _observe(orc, w, para, ids)
+    ctx = fw.FwiContext(para, 0)
+    lam, mu, rho = w.moduli()
+    eager, graph = [], []
+    for enable, out in ((False, eager), (True, graph)):
+        ctx.set_graphs(enable)
+        for scale in (1.0, 1.01, 1.0):
+            out.append(ctx.misfit_grad(lam * scale, mu, rho, w.stf, ids, obs=ref))
+        out.append(ctx.misfit_grad(lam, mu, rho, w.stf, ids[:4], obs=ref[:4]))
+        assert ctx.last_group_count() == 1
+    for a, b in zip(eager, graph):
+        assert a[0] == b[0]
+        for x, y in zip(a[1:], b[1:]):
+            assert np.array_equal(x, y)
+    assert graph[0][0] == graph[2][0] and graph[0][0] != graph[1][0]
+    J_ref = orc.cufd(0, lam, mu, rho, w.stf, ids, para, obs=ref)["misfit"]
+    o = orc.cufd(1, lam, mu, rho, w.stf, ids, para, obs=ref)
+    assert abs(graph[2][0] - J_ref) <= TOL_DATA * abs(J_ref)
+    for k, a in (("g_lambda", graph[2][1]), ("g_mu", graph[2][2]), ("g_den", graph[2][3])):
+        assert rel(a, o[k]) < TOL_GRAD, k
     ctx.close()
