@@ -456,23 +456,17 @@ struct fwigb_ctx {
   size_t fields_stride = 0, store_stride = 0, grads_stride = 0;  // floats per member
   DevBuf g_fields, g_store, g_grads, g_slots;
   int group_cap = 0;
-  // Launch parameters of the current group. A lone shot: one SweepPack<1>
-  // per (sweep variant, tile width), index variant * 3 + tile slot, passed by
-  // value. A batched group: its tensor maps in device memory (g_maps), index
-  // (variant * 3 + tile slot) * group_size + member, and its slots (g_slots),
-  // reached through a SweepTable; maps_host / slots_host are the host copies.
-  int group_size = 0;
+  // Launch parameter packs of the current group: for a lone shot one
+  // SweepPack<1> per (sweep variant, tile width); else one
+  // SweepPack<kPackShots> per (sweep variant, tile width, pack of consecutive
+  // members), index (variant * 3 + tile slot) * npacks + pack. pack_nx[q] is
+  // the widest member sub-grid of pack q.
+  int group_size = 0, npacks = 0;
   std::vector<SweepPack<1>> pack1;
-  DevBuf g_maps, g_tiles;
-  std::vector<TileMaps> maps_host;
-  std::vector<ShotSlot> slots_host;
-  // Per tile shape (rows per thread - 1) * 3 + tile slot, the batched launch's
-  // member prefix first[G + 1] followed by the members' z tile counts ntz[G]
-  // (SweepTable); host copy of g_tiles.
-  std::vector<int> tiles_host;
-  // Launch extent of the group's sweeps: the widest member sub-grid and the
-  // rows down to the last one a member touches.
-  SweepGrid group_grid{0, 0, 0};
+  std::vector<SweepPack<kPackShots>> packs;
+  std::vector<int> pack_nx;
+  // Launch extents per pack.
+  std::vector<SweepGrid> pack_grid;
   int last_groups = 0;
   // CUDA graph of a single-group call's whole launch sequence, replayed while
   // everything it was captured from is unchanged (graph_key).
@@ -1022,9 +1016,9 @@ int plan_groups(fwigb_ctx* ctx, bool adj, std::vector<std::vector<int>>& groups)
 
 // Launches sweep `w` (0 F1, 1 F2, 2 B, 3 C) with `rows` depths per thread
 // (forward sweeps: 1 or 2) over the first `a` members of the current group at
-// tile width tx, in one launch; `arg` is the step (F1) or the backward
-// iteration (B, C); `flags` those of launch_fwd_stress (F1 only). Returns the
-// number of launches.
+// tile width tx, one launch per parameter pack; `arg` is the step (F1) or the
+// backward iteration (B, C); `flags` those of launch_fwd_stress (F1 only).
+// Returns the number of launches.
 int launch_sweep(fwigb_ctx* ctx, int w, int tx, int rows, int a, int arg, int flags, unsigned* d_err) {
   cudaStream_t s = ctx->stream;
   const int variant = rows == 2 ? w + 4 : w;
@@ -1038,20 +1032,19 @@ int launch_sweep(fwigb_ctx* ctx, int w, int tx, int rows, int a, int arg, int fl
     }
   };
   if (a <= 0) return 0;
-  if (ctx->group_size == 1) return go(ctx->pack1[base], 1, ctx->group_grid);
-  const size_t G = static_cast<size_t>(ctx->group_size);
-  const size_t shape = static_cast<size_t>((rows - 1) * 3 + tx_slot(tx)) * (2 * G + 1);
-  const int* first = ctx->g_tiles.as<int>(shape);
-  const SweepTable t{ctx->g_maps.as<TileMaps>(base * G), ctx->g_slots.as<ShotSlot>(), first, first + G + 1, a};
-  return go(t, a, SweepGrid{0, 0, ctx->tiles_host[shape + a]});
+  const SweepGrid* grids = ctx->pack_grid.data();
+  if (ctx->group_size == 1) return go(ctx->pack1[base], 1, grids[0]);
+  int n = 0;
+  for (int q = 0; q * kPackShots < a; ++q)
+    n += go(ctx->packs[base * ctx->npacks + q], std::min(kPackShots, a - q * kPackShots), grids[q]);
+  return n;
 }
 
 // Builds and uploads the slots and tensor maps of a group's members.
 int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
   const size_t ldz = ctx->geo.ldz;
   std::vector<ShotSlot> slots(members.size());
-  const size_t G_ = members.size();
-  std::vector<TileMaps> maps(static_cast<size_t>(kSweepVariants * 3) * G_);
+  std::vector<TileMaps> maps(static_cast<size_t>(kSweepVariants * 3) * ctx->group_cap);
   const int nrm = 0;
   (void)nrm;
   nx_max = 0;
@@ -1115,52 +1108,39 @@ int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
       }
       const TileMaps* per_sweep[kSweepVariants] = {&sm.f1, &sm.f2, &sm.b, &sm.c, &sm.f1w, &sm.f2w, &sm.bw, &sm.cw};
       for (int w = 0; w < kSweepVariants; ++w)
-        maps[static_cast<size_t>(w * 3 + t) * G_ + k] = *per_sweep[w];
+        maps[static_cast<size_t>(w * 3 + t) * ctx->group_cap + k] = *per_sweep[w];
     }
   }
-  // Launch parameters: a lone shot's packs (passed by value at every
-  // launch), or a batched group's table of maps and slots in device memory.
+  // Parameter packs (host; passed by value at every launch).
   const int G = static_cast<int>(members.size());
   ctx->group_size = G;
-  // Launch extent: the widest member sub-grid, and rows down to the last one
-  // a sweep touches (zact1, or the lowest source / receiver row).
-  ctx->group_grid = SweepGrid{0, 0, 0};
+  ctx->npacks = (G + kPackShots - 1) / kPackShots;
+  ctx->pack_nx.assign(ctx->npacks, 0);
+  for (int k = 0; k < G; ++k) ctx->pack_nx[k / kPackShots] = std::max(ctx->pack_nx[k / kPackShots], slots[k].g.nx);
+  // Launch extents: the widest member sub-grid, and rows down to the last
+  // one a sweep touches (zact1, or the lowest source / receiver row).
+  ctx->pack_grid.assign(ctx->npacks, SweepGrid{0, 0});
+  for (int q = 0; q < ctx->npacks; ++q) ctx->pack_grid[q].nx = ctx->pack_nx[q];
   for (int k = 0; k < G; ++k) {
     const int rows = std::min(slots[k].g.nz, std::max(slots[k].g.zact1, slots[k].sh.rbz1) + 1);
-    ctx->group_grid.nz = std::max(ctx->group_grid.nz, rows);
-    ctx->group_grid.nx = std::max(ctx->group_grid.nx, slots[k].g.nx);
+    ctx->pack_grid[k / kPackShots].nz = std::max(ctx->pack_grid[k / kPackShots].nz, rows);
   }
   if (G == 1) {
     ctx->pack1.assign(kSweepVariants * 3, SweepPack<1>{});
     for (int w = 0; w < kSweepVariants * 3; ++w) {
-      ctx->pack1[w].maps[0] = maps[static_cast<size_t>(w)];
+      ctx->pack1[w].maps[0] = maps[static_cast<size_t>(w) * ctx->group_cap];
       ctx->pack1[w].slots[0] = slots[0];
     }
   } else {
-    static_assert(sizeof(TileMaps) % 128 == 0, "tensor maps must stay 64-byte aligned in the table");
-    CK(ctx->g_maps.ensure(maps.size() * sizeof(TileMaps)));
-    CK(cudaMemcpyAsync(ctx->g_maps.p, maps.data(), maps.size() * sizeof(TileMaps), cudaMemcpyHostToDevice,
-                       ctx->stream));
-    // Member tile prefixes of the six tile shapes (1 or 2 rows per thread x 3 widths).
-    ctx->tiles_host.assign(static_cast<size_t>(6) * (2 * G + 1), 0);
-    for (int rr = 1; rr <= 2; ++rr)
-      for (int t = 0; t < 3; ++t) {
-        int* first = ctx->tiles_host.data() + static_cast<size_t>((rr - 1) * 3 + t) * (2 * G + 1);
-        int* ntz = first + G + 1;
-        const int tz = kTileZ * rr, tx = kTileXs[t];
-        for (int k = 0; k < G; ++k) {
-          const int rows = std::min(slots[k].g.nz, std::max(slots[k].g.zact1, slots[k].sh.rbz1) + 1);
-          ntz[k] = (rows + tz - 1) / tz;
-          first[k + 1] = first[k] + ntz[k] * ((slots[k].g.nx + tx - 1) / tx);
-        }
+    ctx->packs.assign(static_cast<size_t>(kSweepVariants * 3) * ctx->npacks, SweepPack<kPackShots>{});
+    for (int w = 0; w < kSweepVariants * 3; ++w)
+      for (int k = 0; k < G; ++k) {
+        SweepPack<kPackShots>& pk = ctx->packs[static_cast<size_t>(w) * ctx->npacks + k / kPackShots];
+        pk.maps[k % kPackShots] = maps[static_cast<size_t>(w) * ctx->group_cap + k];
+        pk.slots[k % kPackShots] = slots[k];
       }
-    CK(ctx->g_tiles.ensure(ctx->tiles_host.size() * sizeof(int)));
-    CK(cudaMemcpyAsync(ctx->g_tiles.p, ctx->tiles_host.data(), ctx->tiles_host.size() * sizeof(int),
-                       cudaMemcpyHostToDevice, ctx->stream));
   }
-  ctx->maps_host = std::move(maps);
-  ctx->slots_host = slots;
-  // Device copy of the slots (the batched sweeps and the gradient reduction).
+  // Device copy of the slots for the gradient reduction.
   CK(cudaMemcpyAsync(ctx->g_slots.p, slots.data(), slots.size() * sizeof(ShotSlot), cudaMemcpyHostToDevice,
                      ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1472,14 +1452,13 @@ int run(fwigb_ctx* ctx, int calc_id) {
     };
     if (ctx->use_graphs && !ctx->timing && groups.size() == 1) {
       // A call of one group (a lone shot, or a batched group of any size) is
-      // replayed from a CUDA graph captured on first use: about 4 launches
-      // per time step (one per sweep for all the group's shots) plus the
-      // residual path. A call of several groups would record a graph per
-      // group and call, so it runs eagerly. The key holds every value the
-      // captured launches depend on: the launch parameters (the lone shot's
-      // packs, or the batched group's table contents and its device address:
-      // pointers, geometry, TMA maps), tile choices, flags, and the members'
-      // data offsets and the buffers of the memsets / residual.
+      // replayed from a CUDA graph captured on first use: per time step one
+      // launch per sweep and parameter pack, plus the residual path. A call of
+      // several groups would record a graph per group and call, so it runs
+      // eagerly. The key holds every value the captured launches depend on:
+      // the parameter packs (pointers, geometry, TMA maps) and launch extents,
+      // tile choices, flags, the members' data offsets and the buffers of the
+      // memsets / residual.
       std::vector<uint64_t> key = {static_cast<uint64_t>(calc_id), static_cast<uint64_t>(ctx->illum),
                                    static_cast<uint64_t>(ctx->per_trace_taper),
                                    static_cast<uint64_t>(ctx->inject_timeout), static_cast<uint64_t>(G)};
@@ -1497,26 +1476,23 @@ int run(fwigb_ctx* ctx, int calc_id) {
                          reinterpret_cast<uint64_t>(ctx->shot_data.p), reinterpret_cast<uint64_t>(ctx->shot_gstf.p),
                          reinterpret_cast<uint64_t>(ctx->shot_taper.p), reinterpret_cast<uint64_t>(ctx->partials.p),
                          reinterpret_cast<uint64_t>(ctx->grads.p), reinterpret_cast<uint64_t>(ctx->scal.p),
-                         reinterpret_cast<uint64_t>(ctx->g_slots.p), reinterpret_cast<uint64_t>(ctx->g_maps.p),
-                         reinterpret_cast<uint64_t>(ctx->g_tiles.p),
-                         reinterpret_cast<uint64_t>(ctx->shot_filt.p), reinterpret_cast<uint64_t>(ctx->filt_tmp.p),
-                         static_cast<uint64_t>(ctx->filt_tmp_floats), static_cast<uint64_t>(ctx->p.if_src_update),
-                         reinterpret_cast<uint64_t>(ctx->shot_supd.p), reinterpret_cast<uint64_t>(ctx->supd_part.p),
-                         reinterpret_cast<uint64_t>(ctx->supd_coef.p), reinterpret_cast<uint64_t>(ctx->supd_k.p)})
+                         reinterpret_cast<uint64_t>(ctx->g_slots.p), reinterpret_cast<uint64_t>(ctx->shot_filt.p),
+                         reinterpret_cast<uint64_t>(ctx->filt_tmp.p), static_cast<uint64_t>(ctx->filt_tmp_floats),
+                         static_cast<uint64_t>(ctx->p.if_src_update), reinterpret_cast<uint64_t>(ctx->shot_supd.p),
+                         reinterpret_cast<uint64_t>(ctx->supd_part.p), reinterpret_cast<uint64_t>(ctx->supd_coef.p),
+                         reinterpret_cast<uint64_t>(ctx->supd_k.p)})
         key.push_back(v);
       auto add_words = [&key](const void* p, size_t bytes) {
         const uint64_t* w = static_cast<const uint64_t*>(p);
         key.insert(key.end(), w, w + bytes / sizeof(uint64_t));
       };
-      static_assert(sizeof(SweepPack<1>) % 8 == 0 && sizeof(TileMaps) % 8 == 0 && sizeof(ShotSlot) % 8 == 0,
+      static_assert(sizeof(SweepPack<1>) % 8 == 0 && sizeof(SweepPack<kPackShots>) % 8 == 0,
                     "launch parameters are compared as 64-bit words");
-      if (G == 1) {
+      if (G == 1)
         add_words(ctx->pack1.data(), ctx->pack1.size() * sizeof(SweepPack<1>));
-      } else {
-        add_words(ctx->maps_host.data(), ctx->maps_host.size() * sizeof(TileMaps));
-        add_words(ctx->slots_host.data(), ctx->slots_host.size() * sizeof(ShotSlot));
-        for (int v : ctx->tiles_host) key.push_back(static_cast<uint64_t>(v));
-      }
+      else
+        add_words(ctx->packs.data(), ctx->packs.size() * sizeof(SweepPack<kPackShots>));
+      for (const SweepGrid& gr : ctx->pack_grid) key.push_back((static_cast<uint64_t>(gr.nz) << 32) | gr.nx);
       if (!ctx->graph_exec || key != ctx->graph_key) {
         if (ctx->graph_exec) {
           cudaGraphExecDestroy(ctx->graph_exec);
@@ -1704,7 +1680,7 @@ int fwigb_destroy(fwigb_ctx* ctx) {
                     &ctx->shot_supd, &ctx->supd_part, &ctx->supd_coef, &ctx->supd_k,
                     &ctx->g_fields,
                     &ctx->g_store, &ctx->g_grads,
-                    &ctx->g_slots, &ctx->g_maps, &ctx->g_tiles})
+                    &ctx->g_slots})
     b->release();
   for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);

@@ -173,34 +173,18 @@ struct SweepMaps {
 // 4 F1, 5 F2, 6 B, 7 C (two rows per thread).
 constexpr int kSweepVariants = 8;
 
-// What one sweep launch reads. A lone shot's launches take its slot and
-// tensor maps by value, as a __grid_constant__ kernel parameter
-// (SweepPack<1>): the blocks read them from the constant bank. A batched
-// group's launches take a SweepTable: pointers to the group's slots and to
-// the tensor maps of the launch's sweep variant and tile width, one per
-// member, in device memory; one launch covers every active member
-// (blockIdx.z), and the kernel parameter stays a few bytes, so the whole
-// group's launch sequence fits a CUDA graph.
+// What one sweep launch reads for up to K shots, passed by value as a
+// __grid_constant__ kernel parameter: the block of shot k reads its slot and
+// tensor maps from the constant bank (no global-memory round trip before its
+// first stencil load). K = 1 for a lone shot; kPackShots for a batch, which
+// keeps the parameter block under the 32 KB kernel-parameter limit.
+constexpr int kPackShots = 16;
 template <int K>
 struct SweepPack {
-  static constexpr bool kLone = (K == 1);
   TileMaps maps[K];
   ShotSlot slots[K];
 };
-struct SweepTable {
-  static constexpr bool kLone = false;
-  const TileMaps* maps;   // [member]: the maps of one sweep variant and tile width
-  const ShotSlot* slots;  // [member]
-  // Tiles of the launch's tile shape, members in order: first[k] is the first
-  // block of member k (first[0] = 0, first[k + 1] - first[k] its tiles) and
-  // ntz[k] its tiles along z. Block b of a launch over the first n members
-  // works on member k with first[k] <= b < first[k + 1], on its tile
-  // b - first[k] (z fastest), so a launch holds no block past a member's own
-  // sub-grid.
-  const int* first;
-  const int* ntz;
-  int n;
-};
+static_assert(sizeof(SweepPack<kPackShots>) < 32000, "sweep pack exceeds the kernel parameter limit");
 
 // Encodes the sweep tensor maps for tile width tx (host; needs the driver's
 // cuTensorMapEncodeTiled). Returns false with a message on failure.
@@ -212,29 +196,28 @@ bool encode_sweep_maps(const Geo& g, const Fields& f, int tx, SweepMaps& out, co
 // Blocks past a shot's own grid leave at once.
 struct SweepGrid {
   int nz, nx;
-  int blocks;  // > 0: a batched launch's 1-D grid of this many blocks (SweepTable::first[n])
 };
 
-// ---- launchers (kernels.cu). One launch covers the first `nshots` shots of
-// a pack (SweepPack<1>: one) or table (SweepTable: the group's active
-// members). err is a device word that a sweep sets when a bounded wait for its
-// staged tiles gives up. The backward sweeps take the backward iteration j;
-// shot k works on its step nSteps_k - 2 - j. Each returns the number of
-// kernels it launched. The launchers take the rows per thread (1 or 2; the
-// maps must be the matching variant). launch_fwd_stress flags: bit 0 saves
-// the boundary ring of step it; bit 1 is the timeout test hook (the sweep's
+// ---- launchers (kernels.cu). One launch covers the first `nshots` (<= K)
+// shots of a pack. err is a device word that a sweep sets when a bounded
+// wait for its staged tiles gives up. The backward sweeps take the backward
+// iteration j; shot k works on its step nSteps_k - 2 - j. Instantiated for
+// K = 1 and K = kPackShots. Each returns the number of kernels it launched.
+// The forward launchers take the rows per thread (1 or 2; the pack's maps
+// must be the matching variant). launch_fwd_stress flags: bit 0 saves the
+// boundary ring of step it; bit 1 is the timeout test hook (the sweep's
 // bounded wait runs out after its tiles have landed and raises err).
-template <class PK>
-int launch_fwd_stress(cudaStream_t s, int tx, int rows, const PK& p, int nshots, const SweepGrid& gr, int it,
-                      int flags, unsigned* err);
-template <class PK>
-int launch_fwd_velocity(cudaStream_t s, int tx, int rows, const PK& p, int nshots, const SweepGrid& gr,
+template <int K>
+int launch_fwd_stress(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
+                      int it, int flags, unsigned* err);
+template <int K>
+int launch_fwd_velocity(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
                         unsigned* err);
-template <class PK>
-int launch_bwd_B(cudaStream_t s, int tx, int rows, const PK& p, int nshots, const SweepGrid& gr, int j,
+template <int K>
+int launch_bwd_B(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err);
-template <class PK>
-int launch_bwd_C(cudaStream_t s, int tx, int rows, const PK& p, int nshots, const SweepGrid& gr, int j,
+template <int K>
+int launch_bwd_C(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err);
 // Adds the per-shot gradients (when g_lam is not null) and illuminations (when
 // g_illum is not null) of the first nshots slots into the global ones.

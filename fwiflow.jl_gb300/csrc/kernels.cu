@@ -105,19 +105,10 @@ __device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* tm, i
 // copies see it) and issues the copies after the block has met the barrier's
 // initialisation; the caller then loads its own-cell operands (which overlap
 // with the copies) and calls stage_wait.
-// GLOBAL: the tensor maps lie in global memory (a batched group's table, which
-// the host rewrites between calls): the issuing thread first acquires each
-// map for the tensor-map proxy (fence.proxy.tensormap::generic.acquire), so
-// the copies never use a stale cached descriptor.
-template <int NA, int TX, int BOXZ, bool GLOBAL = false>
+template <int NA, int TX, int BOXZ>
 __device__ __forceinline__ void stage_issue(const TileMaps& mp, float* sm, uint64_t* bar, int z0, int x0) {
   constexpr int N = BOXZ * (TX + 4);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    if constexpr (GLOBAL) {
-#pragma unroll
-      for (int a = 0; a < NA; ++a)
-        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&mp.t[a]) : "memory");
-    }
     mbar_expect_tx(bar, NA * N * static_cast<unsigned>(sizeof(float)));
 #pragma unroll
     for (int a = 0; a < NA; ++a) tma_load_2d(sm + a * N, &mp.t[a], z0 - 4, x0 - 2, bar);
@@ -129,6 +120,11 @@ __device__ __forceinline__ void stage_init(uint64_t* bar) {
     fence_mbar_init();
   }
   __syncthreads();
+}
+template <int NA, int TX, int BOXZ>
+__device__ __forceinline__ void stage_begin(const TileMaps& mp, float* sm, uint64_t* bar, int z0, int x0) {
+  stage_init(bar);
+  stage_issue<NA, TX, BOXZ>(mp, sm, bar, z0, x0);
 }
 
 // Waits (bounded) for the staged tiles. On a timeout the error word is raised
@@ -240,16 +236,21 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
 // edge tiles, the loads of the media (which no sweep writes) come before the
 // wait and overlap the previous sweep's last blocks.
 #define SWEEP_KERNEL_TILE(TZ_)                                                 \
-  int shot, tzi, txi;                                                          \
-  block_tile(P, shot, tzi, txi);                                               \
+  const int shot = K == 1 ? 0 : static_cast<int>(blockIdx.z);                  \
   const Geo& g0 = P.slots[shot].g;                                             \
-  const int z0 = tzi * (TZ_), x0 = txi * TX;                                   \
+  const int z0 = blockIdx.x * (TZ_), x0 = blockIdx.y * TX;                     \
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");              \
   if (z0 >= g0.nz || x0 >= g0.nx) return;                                      \
   if (z0 > g0.zact1 && !tile_meets_shot_box(P.slots[shot].sh, z0, x0, (TZ_), TX)) return; \
   const TileSplit ts = tile_split(g0, TX, (TZ_));                              \
-  const bool fast = tzi >= ts.ftz0 && tzi < ts.ftz1 && txi >= ts.ftx0 && txi < ts.ftx1; \
-  const bool mid = !fast && tzi >= ts.mtz0 && tzi < ts.mtz1 && txi >= ts.mtx0 && txi < ts.mtx1;
+  const bool fast = static_cast<int>(blockIdx.x) >= ts.ftz0 &&                 \
+                    static_cast<int>(blockIdx.x) < ts.ftz1 &&                  \
+                    static_cast<int>(blockIdx.y) >= ts.ftx0 &&                 \
+                    static_cast<int>(blockIdx.y) < ts.ftx1;                    \
+  const bool mid = !fast && static_cast<int>(blockIdx.x) >= ts.mtz0 &&         \
+                   static_cast<int>(blockIdx.x) < ts.mtz1 &&                   \
+                   static_cast<int>(blockIdx.y) >= ts.mtx0 &&                  \
+                   static_cast<int>(blockIdx.y) < ts.mtx1;
 
 #define SWEEP_BODY_SLOT()                                                      \
   const ShotSlot& S = P.slots[shot];                                           \
@@ -264,31 +265,6 @@ __device__ __forceinline__ int2 bin_range(const ShotD& sh, int z, int x) {
                          x0 + TX - 1 < sh.rbx0 || x0 > sh.rbx1);
 
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-
-// The block's shot and tile (z and x tile indices). A lone shot's launch is a
-// (z tiles, x tiles) grid. A batched launch is a 1-D grid over the tiles of
-// its members: member k owns blocks tiles[k] .. tiles[k+1]-1 (binary search
-// over the member prefix), its tile b - tiles[k] with z fastest.
-__device__ __forceinline__ void block_tile(const SweepPack<1>&, int& shot, int& tzi, int& txi) {
-  shot = 0;
-  tzi = static_cast<int>(blockIdx.x);
-  txi = static_cast<int>(blockIdx.y);
-}
-__device__ __forceinline__ void block_tile(const SweepTable& P, int& shot, int& tzi, int& txi) {
-  const int b = static_cast<int>(blockIdx.x);
-  int lo = 0, hi = P.n;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (__ldg(P.first + mid) <= b)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  const int local = b - __ldg(P.first + lo), ntz = __ldg(P.ntz + lo);
-  shot = lo;
-  tzi = local % ntz;
-  txi = local / ntz;
-}
 
 // Fast tiles: the thread's first cell (z, x), its global index i and its box
 // index b (every cell of a fast tile is inside the grid).
@@ -307,7 +283,7 @@ __device__ __forceinline__ void block_tile(const SweepTable& P, int& shot, int& 
   extern __shared__ __align__(128) float sm[];                                 \
   __shared__ __align__(8) uint64_t bar;                                        \
   stage_init(&bar);
-#define SWEEP_TMA(NA, BOXZ_) stage_issue<NA, TX, (BOXZ_), !PK::kLone>(P.maps[shot], sm, &bar, z0, x0);
+#define SWEEP_TMA(NA, BOXZ_) stage_issue<NA, TX, (BOXZ_)>(P.maps[shot], sm, &bar, z0, x0);
 
 // Edge tiles: the thread's first cell (z, x), its global index i, its box
 // index b and whether the cell lies in the grid (`live`; a thread with no
@@ -359,8 +335,8 @@ __device__ __forceinline__ float dd(float p, float q, float s, float t, float r)
 // recording (utilities.cu:557-567) + from_bnd of the 5 fields (Boundary.cu:55-76).
 // Staged: vz, vx. Edge body: the per-cell code for each of the thread's R
 // depths (after the staged tiles have landed).
-template <int TX, class PK, int R>
-__device__ __forceinline__ void fwd_stress_edge(const PK& P, int shot, int z0, int x0, int it, int save,
+template <int TX, int K, int R>
+__device__ __forceinline__ void fwd_stress_edge(const SweepPack<K>& P, int shot, int z0, int x0, int it, int save,
                                                 bool inject, unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
@@ -442,8 +418,8 @@ __device__ __forceinline__ void fwd_stress_edge(const PK& P, int shot, int z0, i
 }
 
 // F2: el_velocity, isFor = true (el_velocity.cu:45-82). Staged: szz, sxx, sxz.
-template <int TX, class PK, int R>
-__device__ __forceinline__ void fwd_velocity_edge(const PK& P, int shot, int z0, int x0, unsigned* err) {
+template <int TX, int K, int R>
+__device__ __forceinline__ void fwd_velocity_edge(const SweepPack<K>& P, int shot, int z0, int x0, unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
   SWEEP_EDGE_CELL(BOXZ, R)
@@ -492,8 +468,8 @@ __device__ __forceinline__ void fwd_velocity_edge(const PK& P, int shot, int z0,
 // ---------------------------------------------------------------------------
 // B: add_source(-) + el_stress(isFor=false) with the lambda / mu kernels +
 // to_bnd(stress) + el_velocity_adj. Staged: vz, vx, szz_a, sxx_a, sxz_a.
-template <int TX, class PK, int R>
-__device__ __forceinline__ void bwd_B_edge(const PK& P, int shot, int z0, int x0, int j, unsigned* err) {
+template <int TX, int K, int R>
+__device__ __forceinline__ void bwd_B_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
   SWEEP_EDGE_CELL(BOXZ, R)
@@ -640,8 +616,8 @@ __device__ __forceinline__ void bwd_B_edge(const PK& P, int shot, int z0, int x0
 //    + source_grad (utilities.cu:582-593) + el_velocity(isFor=false) with the
 //    density kernel (el_velocity.cu:84-117) + to_bnd(velocity).
 //    Staged: vz_a, vx_a, szz, sxx, sxz.
-template <int TX, class PK, int R>
-__device__ __forceinline__ void bwd_C_edge(const PK& P, int shot, int z0, int x0, int j, unsigned* err) {
+template <int TX, int K, int R>
+__device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int BOXZ = 32 * R + 8;
   SWEEP_BODY_SLOT()
   SWEEP_EDGE_CELL(BOXZ, R)
@@ -791,8 +767,8 @@ __device__ __forceinline__ void bwd_C_edge(const PK& P, int shot, int z0, int x0
 // Forward fast bodies, one depth per thread (32-row tiles).
 // MID: the tile is a mid tile (no CPML cell; it may hold ring cells), and
 // the boundary ring of step it is saved when `save` is set.
-template <int TX, class PK, bool MID>
-__device__ __forceinline__ void fwd_stress_fast1(const PK& P, int shot, int z0, int x0, int it, int save,
+template <int TX, int K, bool MID>
+__device__ __forceinline__ void fwd_stress_fast1(const SweepPack<K>& P, int shot, int z0, int x0, int it, int save,
                                                  bool inject, unsigned* err) {
   SWEEP_FAST_SLOT(kTileZ)
   SWEEP_CELL(kBoxZ, 1)
@@ -835,8 +811,8 @@ __device__ __forceinline__ void fwd_stress_fast1(const PK& P, int shot, int z0, 
   f.sxx[i] = sxx;
 }
 
-template <int TX, class PK>
-__device__ __forceinline__ void fwd_velocity_fast1(const PK& P, int shot, int z0, int x0, unsigned* err) {
+template <int TX, int K>
+__device__ __forceinline__ void fwd_velocity_fast1(const SweepPack<K>& P, int shot, int z0, int x0, unsigned* err) {
   SWEEP_FAST_SLOT(kTileZ)
   (void)special;
   SWEEP_CELL(kBoxZ, 1)
@@ -864,8 +840,8 @@ __device__ __forceinline__ void fwd_velocity_fast1(const PK& P, int shot, int z0
 // operands and results move as float2, and the staged samples are read in
 // pairs (b-2, b-1), (b, b+1), (b+2, b+3) along z and (b, b+1) at each
 // column offset along x, which cover the stencils of both depths.
-template <int TX, class PK, int R, bool MID>
-__device__ __forceinline__ void fwd_stress_fast2(const PK& P, int shot, int z0, int x0, int it, int save,
+template <int TX, int K, int R, bool MID>
+__device__ __forceinline__ void fwd_stress_fast2(const SweepPack<K>& P, int shot, int z0, int x0, int it, int save,
                                                  bool inject, unsigned* err) {
   static_assert(R == 2, "the forward fast bodies handle two depths per thread");
   constexpr int TZ = 32 * R, BOXZ = TZ + 8;
@@ -926,8 +902,8 @@ __device__ __forceinline__ void fwd_stress_fast2(const PK& P, int shot, int z0, 
   st2(f.sxx + i, sxx0, sxx1);
 }
 
-template <int TX, class PK, int R>
-__device__ __forceinline__ void fwd_velocity_fast2(const PK& P, int shot, int z0, int x0, unsigned* err) {
+template <int TX, int K, int R>
+__device__ __forceinline__ void fwd_velocity_fast2(const SweepPack<K>& P, int shot, int z0, int x0, unsigned* err) {
   static_assert(R == 2, "the forward fast bodies handle two depths per thread");
   constexpr int TZ = 32 * R, BOXZ = TZ + 8;
   SWEEP_FAST_SLOT(TZ)
@@ -994,8 +970,8 @@ __device__ __forceinline__ void str(float* p, const float (&v)[R]) {
 // MID: a mid tile (no CPML cell): the reverse stress update and the lambda
 // term only at cells of the reverse-time interior, the ring's stresses of
 // step it restored, and the mu gathers with the guards of the edge form.
-template <int TX, class PK, int R, bool MID>
-__device__ __forceinline__ void bwd_B_fast(const PK& P, int shot, int z0, int x0, int j, unsigned* err) {
+template <int TX, int K, int R, bool MID>
+__device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int TZ = 32 * R, BOXZ = TZ + 8;
   SWEEP_FAST_SLOT(TZ)
   SWEEP_CELL(BOXZ, R)
@@ -1122,8 +1098,8 @@ __device__ __forceinline__ void bwd_B_fast(const PK& P, int shot, int z0, int x0
 // velocity update and its density terms only at cells of the reverse-time
 // interior, the ring's velocities of step it-1 restored, and the density
 // gathers with the guards of the edge form.
-template <int TX, class PK, int R, bool MID>
-__device__ __forceinline__ void bwd_C_fast(const PK& P, int shot, int z0, int x0, int j, unsigned* err) {
+template <int TX, int K, int R, bool MID>
+__device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int TZ = 32 * R, BOXZ = TZ + 8;
   SWEEP_FAST_SLOT(TZ)
   SWEEP_CELL(BOXZ, R)
@@ -1252,8 +1228,8 @@ __device__ __forceinline__ void bwd_C_fast(const PK& P, int shot, int z0, int x0
 // b + o (o even) holds the depths of both cells at offset o, so a z stencil
 // of both depths takes the pairs at b - 2, b, b + 2 and an x stencil the
 // pairs at b + k BOXZ. Operation order per cell is that of the one-row body.
-template <int TX, class PK>
-__device__ __forceinline__ void bwd_B_fast2(const PK& P, int shot, int z0, int x0, int j, unsigned* err) {
+template <int TX, int K>
+__device__ __forceinline__ void bwd_B_fast2(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int TZ = 64, BOXZ = TZ + 8, R = 2;
   SWEEP_FAST_SLOT(TZ)
   SWEEP_CELL(BOXZ, R)
@@ -1359,8 +1335,8 @@ __device__ __forceinline__ void bwd_B_fast2(const PK& P, int shot, int z0, int x
   str<2>(f.vz_a + i, o_vza);
 }
 
-template <int TX, class PK>
-__device__ __forceinline__ void bwd_C_fast2(const PK& P, int shot, int z0, int x0, int j, unsigned* err) {
+template <int TX, int K>
+__device__ __forceinline__ void bwd_C_fast2(const SweepPack<K>& P, int shot, int z0, int x0, int j, unsigned* err) {
   constexpr int TZ = 64, BOXZ = TZ + 8, R = 2;
   SWEEP_FAST_SLOT(TZ)
   SWEEP_CELL(BOXZ, R)
@@ -1474,68 +1450,68 @@ __device__ __forceinline__ void bwd_C_fast2(const PK& P, int shot, int z0, int x
 // picked per workload by the autotuner.
 // flags: bit 0 saves the boundary ring, bit 1 is the timeout test hook
 // (stage_wait's `inject`).
-template <int TX, class PK, int R>
-__global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ PK P, int it, int flags, unsigned* err) {
+template <int TX, int K, int R>
+__global__ void FWD_BOUNDS k_fwd_stress(const __grid_constant__ SweepPack<K> P, int it, int flags, unsigned* err) {
   SWEEP_KERNEL_TILE(32 * R)
   const bool inject = (flags & 2) != 0;
   if (fast) {
     if constexpr (R == 1)
-      fwd_stress_fast1<TX, PK, false>(P, shot, z0, x0, it, 0, inject, err);
+      fwd_stress_fast1<TX, K, false>(P, shot, z0, x0, it, 0, inject, err);
     else
-      fwd_stress_fast2<TX, PK, R, false>(P, shot, z0, x0, it, 0, inject, err);
+      fwd_stress_fast2<TX, K, R, false>(P, shot, z0, x0, it, 0, inject, err);
   } else if (mid) {
     if constexpr (R == 1)
-      fwd_stress_fast1<TX, PK, true>(P, shot, z0, x0, it, flags & 1, inject, err);
+      fwd_stress_fast1<TX, K, true>(P, shot, z0, x0, it, flags & 1, inject, err);
     else
-      fwd_stress_fast2<TX, PK, R, true>(P, shot, z0, x0, it, flags & 1, inject, err);
+      fwd_stress_fast2<TX, K, R, true>(P, shot, z0, x0, it, flags & 1, inject, err);
   } else {
-    fwd_stress_edge<TX, PK, R>(P, shot, z0, x0, it, flags & 1, inject, err);
+    fwd_stress_edge<TX, K, R>(P, shot, z0, x0, it, flags & 1, inject, err);
   }
 }
 
-template <int TX, class PK, int R>
-__global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ PK P, unsigned* err) {
+template <int TX, int K, int R>
+__global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ SweepPack<K> P, unsigned* err) {
   SWEEP_KERNEL_TILE(32 * R)
   // A mid tile of this sweep has nothing beyond the fast form: no CPML cell,
   // every cell in the stencil domain, and no ring or band work.
   if (fast || mid) {
     if constexpr (R == 1)
-      fwd_velocity_fast1<TX, PK>(P, shot, z0, x0, err);
+      fwd_velocity_fast1<TX, K>(P, shot, z0, x0, err);
     else
-      fwd_velocity_fast2<TX, PK, R>(P, shot, z0, x0, err);
+      fwd_velocity_fast2<TX, K, R>(P, shot, z0, x0, err);
   } else {
-    fwd_velocity_edge<TX, PK, R>(P, shot, z0, x0, err);
+    fwd_velocity_edge<TX, K, R>(P, shot, z0, x0, err);
   }
 }
 
 // Backward sweeps: R depths per thread (tiles of 32 R rows), R in {1, 2}.
-template <int TX, class PK, int R>
-__global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ PK P, int j, unsigned* err) {
+template <int TX, int K, int R>
+__global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
   SWEEP_KERNEL_TILE(32 * R)
   if (fast) {
     if constexpr (R == 1)
-      bwd_B_fast<TX, PK, 1, false>(P, shot, z0, x0, j, err);
+      bwd_B_fast<TX, K, 1, false>(P, shot, z0, x0, j, err);
     else
-      bwd_B_fast2<TX, PK>(P, shot, z0, x0, j, err);
+      bwd_B_fast2<TX, K>(P, shot, z0, x0, j, err);
   } else if (mid) {
-    bwd_B_fast<TX, PK, R, true>(P, shot, z0, x0, j, err);
+    bwd_B_fast<TX, K, R, true>(P, shot, z0, x0, j, err);
   } else {
-    bwd_B_edge<TX, PK, R>(P, shot, z0, x0, j, err);
+    bwd_B_edge<TX, K, R>(P, shot, z0, x0, j, err);
   }
 }
 
-template <int TX, class PK, int R>
-__global__ void BWD_BOUNDS k_bwd_C(const __grid_constant__ PK P, int j, unsigned* err) {
+template <int TX, int K, int R>
+__global__ void BWD_BOUNDS k_bwd_C(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
   SWEEP_KERNEL_TILE(32 * R)
   if (fast) {
     if constexpr (R == 1)
-      bwd_C_fast<TX, PK, 1, false>(P, shot, z0, x0, j, err);
+      bwd_C_fast<TX, K, 1, false>(P, shot, z0, x0, j, err);
     else
-      bwd_C_fast2<TX, PK>(P, shot, z0, x0, j, err);
+      bwd_C_fast2<TX, K>(P, shot, z0, x0, j, err);
   } else if (mid) {
-    bwd_C_fast<TX, PK, R, true>(P, shot, z0, x0, j, err);
+    bwd_C_fast<TX, K, R, true>(P, shot, z0, x0, j, err);
   } else {
-    bwd_C_edge<TX, PK, R>(P, shot, z0, x0, j, err);
+    bwd_C_edge<TX, K, R>(P, shot, z0, x0, j, err);
   }
 }
 
@@ -1954,69 +1930,70 @@ void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cu
   cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
-// Launch grid: a lone shot's (z tiles, x tiles); a batched launch's blocks,
-// the tiles of its active members (SweepGrid::blocks, SweepTable::first).
-dim3 sweep_grid(int tx, int tz, const SweepGrid& gr, int) {
-  if (gr.blocks > 0) return dim3(static_cast<unsigned>(gr.blocks), 1, 1);
-  return dim3((gr.nz + tz - 1) / tz, (gr.nx + tx - 1) / tx, 1);
+dim3 sweep_grid(int tx, int tz, const SweepGrid& gr, int nshots) {
+  return dim3((gr.nz + tz - 1) / tz, (gr.nx + tx - 1) / tx, nshots);
 }
 
-template <class PK>
-int launch_fwd_stress(cudaStream_t s, int tx, int rows, const PK& p, int nshots, const SweepGrid& gr, int it,
+template <int K>
+int launch_fwd_stress(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int it,
                       int flags, unsigned* err) {
   const int sv = flags & 3;
   if (rows == 2)
-    FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_stress<TX, PK, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_stress<TX, K, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZFwd>(2), s, p, it, sv, err))
   else
-    FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_stress<TX, PK, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_stress<TX, K, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZ>(2), s, p, it, sv, err))
   return 1;
 }
 
-template <class PK>
-int launch_fwd_velocity(cudaStream_t s, int tx, int rows, const PK& p, int nshots, const SweepGrid& gr,
+template <int K>
+int launch_fwd_velocity(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
                         unsigned* err) {
   if (rows == 2)
-    FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_velocity<TX, PK, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_velocity<TX, K, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZFwd>(3), s, p, err))
   else
-    FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_velocity<TX, PK, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_fwd_velocity<TX, K, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZ>(3), s, p, err))
   return 1;
 }
 
-template <class PK>
-int launch_bwd_B(cudaStream_t s, int tx, int rows, const PK& p, int nshots, const SweepGrid& gr, int j,
+template <int K>
+int launch_bwd_B(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err) {
   if (rows == 2)
-    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, PK, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZFwd>(5), s, p, j, err))
   else
-    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, PK, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZ>(5), s, p, j, err))
   return 1;
 }
 
-template <class PK>
-int launch_bwd_C(cudaStream_t s, int tx, int rows, const PK& p, int nshots, const SweepGrid& gr, int j,
+template <int K>
+int launch_bwd_C(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
                  unsigned* err) {
   if (rows == 2)
-    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, PK, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, K, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZFwd>(5), s, p, j, err))
   else
-    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, PK, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, K, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZ>(5), s, p, j, err))
   return 1;
 }
 
-#define FWIGB_INSTANTIATE(PK)                                                                                   \
-  template int launch_fwd_stress<PK>(cudaStream_t, int, int, const PK&, int, const SweepGrid&, int, int, unsigned*); \
-  template int launch_fwd_velocity<PK>(cudaStream_t, int, int, const PK&, int, const SweepGrid&, unsigned*);         \
-  template int launch_bwd_B<PK>(cudaStream_t, int, int, const PK&, int, const SweepGrid&, int, unsigned*);           \
-  template int launch_bwd_C<PK>(cudaStream_t, int, int, const PK&, int, const SweepGrid&, int, unsigned*);
-FWIGB_INSTANTIATE(SweepPack<1>)
-FWIGB_INSTANTIATE(SweepTable)
+#define FWIGB_INSTANTIATE(K)                                                                                    \
+  template int launch_fwd_stress<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&, int, int,  \
+                                    unsigned*);                                                                  \
+  template int launch_fwd_velocity<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&,        \
+                                      unsigned*);                                                                \
+  template int launch_bwd_B<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&, int,           \
+                               unsigned*);                                                                       \
+  template int launch_bwd_C<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&, int,           \
+                               unsigned*);
+FWIGB_INSTANTIATE(1)
+FWIGB_INSTANTIATE(kPackShots)
 #undef FWIGB_INSTANTIATE
 
 // Tensor maps: one per staged array, a 2-D view (z inner, x outer; row stride

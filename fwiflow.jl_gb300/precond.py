@@ -15,11 +15,16 @@ g * gain directly lets the bright cells dominate.
 Every arithmetic step of the network runs in the library's own sm_103a
 kernels (csrc/cnn.cu: BF16 tensor-core convolutions with FP32 accumulation,
 weight gradients, masked MSE, Adam); torch tensors only hold the device
-memory, and the torch current stream is the one the kernels run on. With
-use_tc (the default) the convolutions with 32 outputs -- the first five
-layers and every data gradient -- run on tcgen05 (tensor memory
-accumulators); the 3-output head and the weight gradients on warp-level
-mma.sync.
+memory, and the torch current stream is the one the kernels run on. The
+convolutions with 32 outputs -- the first five layers and every data
+gradient -- have two kernels: a persistent warp-specialised tcgen05 kernel
+(TMA-fed input ring, tensor-memory accumulators; use_tc=True) and a
+warp-level mma.sync kernel (the default). Measured on GB300 (32 -> 32
+channels, benchmark_convs) the mma.sync kernel is the faster at every image
+size tried (188 / 203 / 222 against 138 / 182 / 212 TFLOP/s on 352 x 832 /
+608 x 1600 / 1120 x 3152 pixels): both are bound by the input loads and the
+GELU epilogue, not the tensor pipe. The 3-output head and the weight
+gradients always run on mma.sync.
 
 Image layout of the kernels: pixel p = x * Hz + z (z fastest), channels
 innermost; a model-shaped array (nz, nx) maps to it by transposition.
@@ -96,7 +101,7 @@ class CnnPreconditioner:
     # (real in, real out, padded in, padded out) per layer
     LAYERS = [(N_IN, WIDTH, 16, 32)] + [(WIDTH, WIDTH, 32, 32)] * (DEPTH - 2) + [(WIDTH, N_OUT, 32, 16)]
 
-    def __init__(self, Hz: int, Wx: int, seed: int = 0, device: int = 0, use_tc: bool = True):
+    def __init__(self, Hz: int, Wx: int, seed: int = 0, device: int = 0, use_tc: bool = False):
         torch = _torch()
         self.use_tc = use_tc
         if Hz % 32:

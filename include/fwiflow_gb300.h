@@ -182,11 +182,12 @@ int fwigb_set_tile_config(fwigb_ctx *ctx, const int *tile_x);
 int fwigb_tile_rows(const fwigb_ctx *ctx, int *rows);
 int fwigb_set_tile_rows(fwigb_ctx *ctx, const int *rows);
 
-/* CUDA graphs (on by default): a run whose shots form a single group of one
- * shot records its whole launch sequence (about 4 launches per time step) into a
- * CUDA graph the first time and replays it while the staged shot, the model
- * and data buffers and the tile choices are unchanged; per-kernel timing
- * runs eagerly. enable = 0 runs every call eagerly. */
+/* CUDA graphs (on by default): a run whose shots form a single group (one
+ * shot, or a batched group) records its whole launch sequence (per time step
+ * one launch per sweep and pack of up to 16 shots: about 4 for a lone shot)
+ * into a CUDA graph the first time and replays it while the staged shots, the
+ * model and data buffers and the tile choices are unchanged; per-kernel
+ * timing runs eagerly. enable = 0 runs every call eagerly. */
 int fwigb_set_graphs(fwigb_ctx *ctx, int enable);
 
 /* Average duration of one launch of sweep `kind` (0 forward stress, 1 forward
