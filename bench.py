@@ -22,8 +22,9 @@ call (an event pair around each sweep step, all shot packs of the step).
 `--impl reference` times the reference algorithm's CPU implementation (the
 oracle restatement, all host threads) on a bounded number of time steps of
 the same workload. `cpu_baseline` (N = 1 only): the same oracle on the
-first steps of the same workload. With N > 1 (torchrun) every rank runs
-its own replica.
+first steps of the same workload. With N > 1 (torchrun) the multi-shot
+workloads grow to N times their shots and each rank runs its cost-balanced
+share (weak scaling); the single-shot workloads run one replica per rank.
 Shots with their own aperture window and record length count their own
 cells and steps.
 """

@@ -1,7 +1,7 @@
 """Batched shots on the sm_103a path: shots with their own aperture window and
-record length, run as concurrent groups (one launch per sweep and time step
-covers every active shot of the group, which reads its slot and tensor maps
-from a device table; a one-group call replays from a CUDA graph).
+record length, run as concurrent groups (each sweep launch covers a pack of
+up to 16 shots of the group, whose slots and tensor maps travel as the
+kernel parameter; a one-group call replays from a CUDA graph).
 
 A windowed shot is defined as the reference run alone on the shot's sub-model
 (padded columns win_x0 .. win_x1 + 2 nPml) for its own record length, its
@@ -169,9 +169,8 @@ def test_illumination_matches_oracle(gpu_lib, fw, orc, tmp_path):
 
 
 def test_batched_graph_replay_is_identical(gpu_lib, fw, orc, tmp_path):
-    """A batched group (one launch per sweep step for all its shots, reading
-    their slots and tensor maps from a device table) replays its whole call
-    from a CUDA graph: same bits as eager launches, across a model change
+    """A batched group (its shots' slots and tensor maps in the parameter pack
+    of each sweep launch) replays its whole call from a CUDA graph: same bits as eager launches, across a model change
     (replay) and a different shot set (re-recorded); and the replayed call
     matches the oracle."""
     w = uneven_tiny(n_shots=6, seed=17)
