@@ -349,6 +349,7 @@ def main():
     launches_per_step = ctx.last_launch_count()
     cfg["tile_widths"] = dict(zip(SWEEP_NAMES, ctx.tile_config()))
     cfg["tile_rows_per_thread"] = dict(zip(SWEEP_NAMES, ctx.tile_rows()))
+    cfg["tile_registers"] = dict(zip(SWEEP_NAMES, ctx.tile_registers()))
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, stops)]
     dev_s = sum(step_ms) / 1e3
     if world > 1:

@@ -59,6 +59,8 @@ SIGNATURES = {
     "fwigb_set_kernel_timing": ([_V, ctypes.c_int], ctypes.c_int),
     "fwigb_tile_config": ([_V, _I], ctypes.c_int),
     "fwigb_tile_rows": ([_V, _I], ctypes.c_int),
+    "fwigb_tile_registers": ([_V, _I], ctypes.c_int),
+    "fwigb_set_tile_registers": ([_V, _I], ctypes.c_int),
     "fwigb_set_tile_rows": ([_V, _I], ctypes.c_int),
     "fwigb_set_graphs": ([_V, ctypes.c_int], ctypes.c_int),
     "fwigb_sweep_time": ([_V, ctypes.c_int, ctypes.c_int, _D], ctypes.c_int),

@@ -481,6 +481,7 @@ struct fwigb_ctx {
   long long launches = 0;
   int tx[4] = {8, 8, 8, 8};    // tile width per sweep (F1, F2, B, C)
   int rows[4] = {2, 2, 1, 1};  // depths per thread per sweep (1 or 2)
+  int regs[4] = {32, 32, 32, 32};  // register budget of the backward sweeps' one-row tiles (32 or 40)
   bool tuned_fwd = false, tuned_bwd = false;
   bool autotune = true;
   // Timeout test hook: the first forward sweep of every run lets its bounded
@@ -1027,8 +1028,8 @@ int launch_sweep(fwigb_ctx* ctx, int w, int tx, int rows, int a, int arg, int fl
     switch (w) {
       case 0: return launch_fwd_stress(s, tx, rows, pk, n, gr, arg, flags, d_err);
       case 1: return launch_fwd_velocity(s, tx, rows, pk, n, gr, d_err);
-      case 2: return launch_bwd_B(s, tx, rows, pk, n, gr, arg, d_err);
-      default: return launch_bwd_C(s, tx, rows, pk, n, gr, arg, d_err);
+      case 2: return launch_bwd_B(s, tx, rows, ctx->regs[2], pk, n, gr, arg, d_err);
+      default: return launch_bwd_C(s, tx, rows, ctx->regs[3], pk, n, gr, arg, d_err);
     }
   };
   if (a <= 0) return 0;
@@ -1150,7 +1151,7 @@ int build_group(fwigb_ctx* ctx, const std::vector<int>& members, int& nx_max) {
 // Tile autotuner: times every candidate tile of each sweep on the first
 // group of the first run (on its live buffers, which the run then resets) and
 // keeps the fastest: widths 4, 8, 16 for every sweep, times 1 or 2 depths per
-// thread for the forward sweeps. The candidates are timed interleaved over
+// thread, and for the backward sweeps' one-row tiles 32 or 40 registers. The candidates are timed interleaved over
 // several rounds and each keeps its best time, so a transient on the GPU does
 // not decide the choice. The backward sweeps are tuned on the first run with
 // the adjoint.
@@ -1158,15 +1159,18 @@ int autotune(fwigb_ctx* ctx, int nshots, int nx_max, bool adj) {
   cudaStream_t s = ctx->stream;
   unsigned* d_err = reinterpret_cast<unsigned*>(ctx->scal.as<char>() + 16);
   (void)nx_max;
-  constexpr int kRounds = 4, kReps = 5, kMaxCand = 6;
+  constexpr int kRounds = 4, kReps = 5, kMaxCand = 9;
   std::vector<cudaEvent_t> ev(2 * kRounds * kMaxCand);
   for (cudaEvent_t& e : ev) CK(cudaEventCreate(&e));
   const int kinds_end = (adj && ctx->nSteps_max >= 2) ? 4 : 2;
   for (int kind = ctx->tuned_fwd ? 2 : 0; kind < kinds_end; ++kind) {
-    const int ncand = 6;  // (width, rows) candidates
+    // (width, rows) candidates; the backward sweeps add one-row tiles at 40
+    // registers (ctx->regs, read by launch_sweep, is set per candidate).
+    const int ncand = kind >= 2 ? 9 : 6;
     auto cand = [&](int q, int& tx, int& rows) {
       tx = kTileXs[q % 3];
-      rows = q < 3 ? 1 : 2;
+      rows = (q / 3) == 1 ? 2 : 1;
+      ctx->regs[kind] = (q / 3) == 2 ? 40 : 32;
     };
     for (int q = 0; q < ncand; ++q) {  // warm-up
       int tx, rows;
@@ -1183,6 +1187,7 @@ int autotune(fwigb_ctx* ctx, int nshots, int nx_max, bool adj) {
       }
     CK(cudaStreamSynchronize(s));
     float best = 1e30f;
+    int qbest = 0;
     for (int q = 0; q < ncand; ++q) {
       float t = 1e30f;
       for (int r = 0; r < kRounds; ++r) {
@@ -1192,9 +1197,10 @@ int autotune(fwigb_ctx* ctx, int nshots, int nx_max, bool adj) {
       }
       if (t < best) {
         best = t;
-        cand(q, ctx->tx[kind], ctx->rows[kind]);
+        qbest = q;
       }
     }
+    cand(qbest, ctx->tx[kind], ctx->rows[kind]);
   }
   CK(cudaGetLastError());
   for (cudaEvent_t e : ev) cudaEventDestroy(e);
@@ -1462,7 +1468,9 @@ int run(fwigb_ctx* ctx, int calc_id) {
       std::vector<uint64_t> key = {static_cast<uint64_t>(calc_id), static_cast<uint64_t>(ctx->illum),
                                    static_cast<uint64_t>(ctx->per_trace_taper),
                                    static_cast<uint64_t>(ctx->inject_timeout), static_cast<uint64_t>(G)};
-      for (int k = 0; k < 4; ++k) key.push_back((static_cast<uint64_t>(ctx->tx[k]) << 8) | ctx->rows[k]);
+      for (int k = 0; k < 4; ++k)
+        key.push_back((static_cast<uint64_t>(ctx->regs[k]) << 16) | (static_cast<uint64_t>(ctx->tx[k]) << 8) |
+                      ctx->rows[k]);
       for (int k = 0; k < G; ++k) {
         const ShotPlan& pl = ctx->plans[mem[k]];
         for (uint64_t v : {static_cast<uint64_t>(pl.nrec), static_cast<uint64_t>(pl.nSteps),
@@ -1815,6 +1823,26 @@ int fwigb_set_graphs(fwigb_ctx* ctx, int enable) {
 int fwigb_tile_rows(const fwigb_ctx* ctx, int* rows) {
   if (!ctx || !rows) return FWIGB_ERR_ARG;
   for (int k = 0; k < 4; ++k) rows[k] = ctx->rows[k];
+  return FWIGB_OK;
+}
+
+int fwigb_tile_registers(const fwigb_ctx* ctx, int* regs) {
+  if (!ctx || !regs) return FWIGB_ERR_ARG;
+  for (int k = 0; k < 4; ++k) regs[k] = k >= 2 && ctx->rows[k] == 1 ? ctx->regs[k] : (k >= 2 ? 64 : 32);
+  return FWIGB_OK;
+}
+
+int fwigb_set_tile_registers(fwigb_ctx* ctx, const int* regs) {
+  if (!ctx || !regs) return FWIGB_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  for (int k = 2; k < 4; ++k)
+    if (regs[k] != 32 && regs[k] != 40) {
+      ctx->err = "backward one-row tiles run at 32 or 40 registers";
+      return FWIGB_ERR_ARG;
+    }
+  ctx->regs[2] = regs[2];
+  ctx->regs[3] = regs[3];
+  ctx->autotune = false;
   return FWIGB_OK;
 }
 

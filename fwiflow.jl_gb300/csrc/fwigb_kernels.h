@@ -213,12 +213,14 @@ int launch_fwd_stress(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, i
 template <int K>
 int launch_fwd_velocity(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
                         unsigned* err);
+// The backward launchers also take the register budget of one-row tiles:
+// 32 (64 warps per SM) or 40 (48 warps per SM); two-row tiles use 64.
 template <int K>
-int launch_bwd_B(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
-                 unsigned* err);
+int launch_bwd_B(cudaStream_t s, int tx, int rows, int regs, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
+                 int j, unsigned* err);
 template <int K>
-int launch_bwd_C(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
-                 unsigned* err);
+int launch_bwd_C(cudaStream_t s, int tx, int rows, int regs, const SweepPack<K>& p, int nshots, const SweepGrid& gr,
+                 int j, unsigned* err);
 // Adds the per-shot gradients (when g_lam is not null) and illuminations (when
 // g_illum is not null) of the first nshots slots into the global ones.
 void launch_reduce_grads(cudaStream_t s, int nz, int nx, int ldz, int nshots, const ShotSlot* slots, float* g_lam,

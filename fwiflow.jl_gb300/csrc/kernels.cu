@@ -321,14 +321,16 @@ __device__ __forceinline__ float dd(float p, float q, float s, float t, float r)
 }
 
 // Register budgets (measured on GB300 over the tile widths; the sweeps wait
-// on memory latency, so resident warps count for more than the few bytes
+// on memory latency, so resident warps count for more than the bytes
 // spilled): forward sweeps 32 registers (64 warps per SM; with two cells per
-// thread 9 % faster than 40 registers on a 16-shot group); backward sweeps 40
-// with one cell (48 warps per SM: 8 % faster than 48 registers) and 64 with
-// two (32 warps per SM).
+// thread 9 % faster than 40 registers on a 16-shot group). Backward sweeps:
+// NT resident threads per SM, so 65536 / NT registers: with one cell per
+// thread 2048 (32 registers, 52-96 bytes spilled; 4 % faster than 40 on the
+// 64-shot workload) or 1536 (40 registers; 10 % faster on a lone 608 x 1600
+// shot, whose arrays stay partly in L2), picked by the autotuner; with two
+// cells 1024 (64 registers).
 #define FWD_BOUNDS __launch_bounds__(32 * TX, 2048 / (32 * TX))
-#define BWD_BOUNDS \
-  __launch_bounds__(32 * TX, ((R == 1 ? 1536 : 1024) / (32 * TX)) > 0 ? ((R == 1 ? 1536 : 1024) / (32 * TX)) : 1)
+#define BWD_BOUNDS __launch_bounds__(32 * TX, (NT / (32 * TX)) > 0 ? (NT / (32 * TX)) : 1)
 
 // ---------------------------------------------------------------------------
 // F1: el_stress (el_stress.cu:50-88) + add_source (utilities.cu:521-541) +
@@ -1484,8 +1486,9 @@ __global__ void FWD_BOUNDS k_fwd_velocity(const __grid_constant__ SweepPack<K> P
   }
 }
 
-// Backward sweeps: R depths per thread (tiles of 32 R rows), R in {1, 2}.
-template <int TX, int K, int R>
+// Backward sweeps: R depths per thread (tiles of 32 R rows), R in {1, 2};
+// NT resident threads per SM (the register budget, BWD_BOUNDS).
+template <int TX, int K, int R, int NT>
 __global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
   SWEEP_KERNEL_TILE(32 * R)
   if (fast) {
@@ -1500,7 +1503,7 @@ __global__ void BWD_BOUNDS k_bwd_B(const __grid_constant__ SweepPack<K> P, int j
   }
 }
 
-template <int TX, int K, int R>
+template <int TX, int K, int R, int NT>
 __global__ void BWD_BOUNDS k_bwd_C(const __grid_constant__ SweepPack<K> P, int j, unsigned* err) {
   SWEEP_KERNEL_TILE(32 * R)
   if (fast) {
@@ -1960,25 +1963,31 @@ int launch_fwd_velocity(cudaStream_t s, int tx, int rows, const SweepPack<K>& p,
 }
 
 template <int K>
-int launch_bwd_B(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
-                 unsigned* err) {
+int launch_bwd_B(cudaStream_t s, int tx, int rows, int regs, const SweepPack<K>& p, int nshots,
+                 const SweepGrid& gr, int j, unsigned* err) {
   if (rows == 2)
-    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K, 2, 1024>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZFwd>(5), s, p, j, err))
+  else if (regs > 32)
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K, 1, 1536>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+                                     smem_bytes<TX, kBoxZ>(5), s, p, j, err))
   else
-    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K, 1, 2048>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZ>(5), s, p, j, err))
   return 1;
 }
 
 template <int K>
-int launch_bwd_C(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int nshots, const SweepGrid& gr, int j,
-                 unsigned* err) {
+int launch_bwd_C(cudaStream_t s, int tx, int rows, int regs, const SweepPack<K>& p, int nshots,
+                 const SweepGrid& gr, int j, unsigned* err) {
   if (rows == 2)
-    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, K, 2>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, K, 2, 1024>, sweep_grid(TX, kTileZFwd, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZFwd>(5), s, p, j, err))
+  else if (regs > 32)
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, K, 1, 1536>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+                                     smem_bytes<TX, kBoxZ>(5), s, p, j, err))
   else
-    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, K, 1>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
+    FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_C<TX, K, 1, 2048>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
                                      smem_bytes<TX, kBoxZ>(5), s, p, j, err))
   return 1;
 }
@@ -1988,9 +1997,9 @@ int launch_bwd_C(cudaStream_t s, int tx, int rows, const SweepPack<K>& p, int ns
                                     unsigned*);                                                                  \
   template int launch_fwd_velocity<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&,        \
                                       unsigned*);                                                                \
-  template int launch_bwd_B<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&, int,           \
+  template int launch_bwd_B<K>(cudaStream_t, int, int, int, const SweepPack<K>&, int, const SweepGrid&, int,      \
                                unsigned*);                                                                       \
-  template int launch_bwd_C<K>(cudaStream_t, int, int, const SweepPack<K>&, int, const SweepGrid&, int,           \
+  template int launch_bwd_C<K>(cudaStream_t, int, int, int, const SweepPack<K>&, int, const SweepGrid&, int,      \
                                unsigned*);
 FWIGB_INSTANTIATE(1)
 FWIGB_INSTANTIATE(kPackShots)

@@ -218,6 +218,18 @@ class FwiContext:
         _lib.check(self._lib.fwigb_tile_rows(self._h, _lib.iptr(t)), self._h)
         return [int(v) for v in t]
 
+    def tile_registers(self):
+        """Registers per thread of the four sweeps' tiles (the backward one-row
+        tiles run at 32 or 40, picked by the autotuner)."""
+        t = np.zeros(4, dtype=np.int32)
+        _lib.check(self._lib.fwigb_tile_registers(self._h, _lib.iptr(t)), self._h)
+        return [int(v) for v in t]
+
+    def set_tile_registers(self, regs) -> None:
+        """Fix the backward sweeps' one-row register budget (entries 2, 3: 32 or 40)."""
+        t = np.ascontiguousarray(regs, dtype=np.int32)
+        _lib.check(self._lib.fwigb_set_tile_registers(self._h, _lib.iptr(t)), self._h)
+
     def set_tile_config(self, widths=None) -> None:
         """Fix the four tile widths (4, 8 or 16); None re-enables the autotuner."""
         t = None if widths is None else np.ascontiguousarray(widths, dtype=np.int32)

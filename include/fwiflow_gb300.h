@@ -180,6 +180,14 @@ int fwigb_test_inject_wait_timeout(fwigb_ctx *ctx, int enable);
 int fwigb_tile_config(const fwigb_ctx *ctx, int *tile_x);
 int fwigb_set_tile_config(fwigb_ctx *ctx, const int *tile_x);
 int fwigb_tile_rows(const fwigb_ctx *ctx, int *rows);
+
+/* Registers per thread of the four sweeps' tiles: the forward sweeps run at
+ * 32, the backward sweeps' two-row tiles at 64 and their one-row tiles at 32
+ * or 40, which the autotuner picks with the widths (32 until it has run).
+ * fwigb_set_tile_registers fixes the backward one-row budget (entries 2 and 3:
+ * 32 or 40; entries 0 and 1 are ignored) and stops the tuning. */
+int fwigb_tile_registers(const fwigb_ctx *ctx, int *regs);
+int fwigb_set_tile_registers(fwigb_ctx *ctx, const int *regs);
 int fwigb_set_tile_rows(fwigb_ctx *ctx, const int *rows);
 
 /* CUDA graphs (on by default): a run whose shots form a single group (one

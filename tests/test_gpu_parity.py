@@ -121,17 +121,21 @@ def test_every_tile_shape_with_deep_source_and_receivers(gpu_lib, fw, orc, tmp_p
     r1 = orc.cufd(1, lam, mu, rho, w.stf, ids, para)
     J0 = orc.cufd(0, lam, mu, rho, w.stf, ids, para)["misfit"]
     ctx = fw.FwiContext(para, 0)
-    for width in (4, 8, 16):
-        for rows in (1, 2):
-            ctx.set_tile_config([width] * 4)
-            ctx.set_tile_rows([rows] * 4)
-            got = ctx.obs(lo, mo, ro, w.stf, ids, write_files=False)
-            for a, b in zip(got, ref):
-                assert rel(a, b) < TOL_DATA, (width, rows)
-            J, gl, gm, gd, gs = ctx.misfit_grad(lam, mu, rho, w.stf, ids)
-            assert abs(J - J0) <= TOL_DATA * abs(J0), (width, rows)
-            for k, a in (("g_lambda", gl), ("g_mu", gm), ("g_den", gd), ("g_stf", gs)):
-                assert rel(a, r1[k]) < TOL_GRAD, (k, width, rows)
+    # one-row backward tiles at both register budgets (32, 40); two-row tiles run at 64
+    for width, rows, regs in [(wd, r, 32) for wd in (4, 8, 16) for r in (1, 2)] + [(wd, 1, 40) for wd in (4, 8, 16)]:
+        ctx.set_tile_config([width] * 4)
+        ctx.set_tile_rows([rows] * 4)
+        ctx.set_tile_registers([32, 32, regs, regs])
+        assert ctx.tile_registers()[2:] == ([regs, regs] if rows == 1 else [64, 64])
+        got = ctx.obs(lo, mo, ro, w.stf, ids, write_files=False)
+        for a, b in zip(got, ref):
+            assert rel(a, b) < TOL_DATA, (width, rows)
+        J, gl, gm, gd, gs = ctx.misfit_grad(lam, mu, rho, w.stf, ids)
+        assert abs(J - J0) <= TOL_DATA * abs(J0), (width, rows, regs)
+        for k, a in (("g_lambda", gl), ("g_mu", gm), ("g_den", gd), ("g_stf", gs)):
+            assert rel(a, r1[k]) < TOL_GRAD, (k, width, rows, regs)
+    with pytest.raises(Exception):
+        ctx.set_tile_registers([32, 32, 48, 32])
     ctx.close()
 
 
