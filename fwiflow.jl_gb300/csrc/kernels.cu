@@ -769,13 +769,45 @@ __device__ __forceinline__ void bwd_C_edge(const SweepPack<K>& P, int shot, int 
 // Forward fast bodies, one depth per thread (32-row tiles).
 // MID: the tile is a mid tile (no CPML cell; it may hold ring cells), and
 // the boundary ring of step it is saved when `save` is set.
+// The media arrays are read by every sweep and, in a batched launch, by every
+// shot of the pack (their sub-grids are windows of the same model): their
+// loads carry an L2 evict-last policy so that the streamed fields do not push
+// them out of L2 (createpolicy / ld.global.L2::cache_hint).
+__device__ __forceinline__ uint64_t media_policy() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ float ldm(const float* a, uint64_t pol) {
+  float v;
+  asm("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float2 ldm2(const float* a, uint64_t pol) {
+  float2 v;
+  asm("ld.global.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(a), "l"(pol));
+  return v;
+}
+template <int R>
+__device__ __forceinline__ void ldrm(const float* p, float (&v)[R], uint64_t pol) {
+  if constexpr (R == 2) {
+    const float2 t = ldm2(p, pol);
+    v[0] = t.x;
+    v[1] = t.y;
+  } else {
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = ldm(p + r, pol);
+  }
+}
+
 template <int TX, int K, bool MID>
 __device__ __forceinline__ void fwd_stress_fast1(const SweepPack<K>& P, int shot, int z0, int x0, int it, int save,
                                                  bool inject, unsigned* err) {
   SWEEP_FAST_SLOT(kTileZ)
   SWEEP_CELL(kBoxZ, 1)
   SWEEP_SMEM(kBoxZ)
-  const float lam = m.lam[i], l2m = m.l2m[i], amu = m.aveMu[i];
+  const uint64_t pol = media_policy();
+  const float lam = ldm(m.lam + i, pol), l2m = ldm(m.l2m + i, pol), amu = ldm(m.aveMu + i, pol);
   pdl_wait();
   SWEEP_TMA(2, kBoxZ)
   float szz = f.szz[i], sxx = f.sxx[i];
@@ -819,7 +851,8 @@ __device__ __forceinline__ void fwd_velocity_fast1(const SweepPack<K>& P, int sh
   (void)special;
   SWEEP_CELL(kBoxZ, 1)
   SWEEP_SMEM(kBoxZ)
-  const float bA = m.bycA[i], bB = m.bycB[i];
+  const uint64_t pol = media_policy();
+  const float bA = ldm(m.bycA + i, pol), bB = ldm(m.bycB + i, pol);
   pdl_wait();
   SWEEP_TMA(3, kBoxZ)
   const float vz = f.vz[i], vx = f.vx[i];
@@ -850,7 +883,8 @@ __device__ __forceinline__ void fwd_stress_fast2(const SweepPack<K>& P, int shot
   SWEEP_FAST_SLOT(TZ)
   SWEEP_CELL(BOXZ, R)
   SWEEP_SMEM(BOXZ)
-  const float2 lam = ld2(m.lam + i), l2m = ld2(m.l2m + i), amu = ld2(m.aveMu + i);
+  const uint64_t pol = media_policy();
+  const float2 lam = ldm2(m.lam + i, pol), l2m = ldm2(m.l2m + i, pol), amu = ldm2(m.aveMu + i, pol);
   pdl_wait();
   SWEEP_TMA(2, BOXZ)
   const float2 szz = ld2(f.szz + i), sxx = ld2(f.sxx + i), sxz = ld2(f.sxz + i);
@@ -912,7 +946,8 @@ __device__ __forceinline__ void fwd_velocity_fast2(const SweepPack<K>& P, int sh
   (void)special;
   SWEEP_CELL(BOXZ, R)
   SWEEP_SMEM(BOXZ)
-  const float2 bA = ld2(m.bycA + i), bB = ld2(m.bycB + i);
+  const uint64_t pol = media_policy();
+  const float2 bA = ldm2(m.bycA + i, pol), bB = ldm2(m.bycB + i, pol);
   pdl_wait();
   SWEEP_TMA(3, BOXZ)
   const float2 vz = ld2(f.vz + i), vx = ld2(f.vx + i);
@@ -982,13 +1017,14 @@ __device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int 
   const int it = S.nSteps - 2 - j;
   const float dt = g.dt;
   float szz[R], sxx[R], sxz[R], lam[R], l2m[R], amu[R], gl[R], gm[R], w[R], h[R], va_z[R], va_x[R], hx[R];
-  ldr<R>(m.lam + i, lam);
-  ldr<R>(m.l2m + i, l2m);
-  ldr<R>(m.aveMu + i, amu);
-  ldr<R>(m.muw + i, w);
-  ldr<R>(m.hs + i, h);
-  ldr<R>(m.hs + i - ldz, hx);
-  const float hz0 = m.hs[i - 1], hzx0 = m.hs[i - ldz - 1];
+  const uint64_t pol = media_policy();
+  ldrm<R>(m.lam + i, lam, pol);
+  ldrm<R>(m.l2m + i, l2m, pol);
+  ldrm<R>(m.aveMu + i, amu, pol);
+  ldrm<R>(m.muw + i, w, pol);
+  ldrm<R>(m.hs + i, h, pol);
+  ldrm<R>(m.hs + i - ldz, hx, pol);
+  const float hz0 = ldm(m.hs + i - 1, pol), hzx0 = ldm(m.hs + i - ldz - 1, pol);
   pdl_wait();
   SWEEP_TMA(5, BOXZ)
   ldr<R>(f.szz + i, szz);
@@ -1111,8 +1147,9 @@ __device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int 
   const int rev = it >= 1;
   const float dt = g.dt;
   float sa[R], xa[R], za[R], bA[R], bB[R], vz[R], vx[R], gd[R], bBj[R];
-  ldr<R>(m.bycA + i, bA);
-  ldr<R>(m.bycB + i, bB);
+  const uint64_t pol = media_policy();
+  ldrm<R>(m.bycA + i, bA, pol);
+  ldrm<R>(m.bycB + i, bB, pol);
   pdl_wait();
   SWEEP_TMA(5, BOXZ)
   ldr<R>(f.szz_a + i, sa);
@@ -1125,8 +1162,8 @@ __device__ __forceinline__ void bwd_C_fast(const SweepPack<K>& P, int shot, int 
     ldr<R>(f.vz + i, vz);
     ldr<R>(f.vx + i, vx);
     ldr<R>(gr.den + i, gd);
-    ldr<R>(m.bycB + i - ldz, bBj);
-    bAj0 = m.bycA[i - 1];
+    ldrm<R>(m.bycB + i - ldz, bBj, pol);
+    bAj0 = ldm(m.bycA + i - 1, pol);
   }
   if (!stage_wait(&bar, err)) return;
   const float* s_vz_a = sm;
@@ -1240,13 +1277,14 @@ __device__ __forceinline__ void bwd_B_fast2(const SweepPack<K>& P, int shot, int
   const int it = S.nSteps - 2 - j;
   const float dt = g.dt;
   float szz[2], sxx[2], sxz[2], lam[2], l2m[2], amu[2], gl[2], gm[2], w[2], h[2], va_z[2], va_x[2], hx[2];
-  ldr<2>(m.lam + i, lam);
-  ldr<2>(m.l2m + i, l2m);
-  ldr<2>(m.aveMu + i, amu);
-  ldr<2>(m.muw + i, w);
-  ldr<2>(m.hs + i, h);
-  ldr<2>(m.hs + i - ldz, hx);
-  const float hz0 = m.hs[i - 1], hzx0 = m.hs[i - ldz - 1];
+  const uint64_t pol = media_policy();
+  ldrm<2>(m.lam + i, lam, pol);
+  ldrm<2>(m.l2m + i, l2m, pol);
+  ldrm<2>(m.aveMu + i, amu, pol);
+  ldrm<2>(m.muw + i, w, pol);
+  ldrm<2>(m.hs + i, h, pol);
+  ldrm<2>(m.hs + i - ldz, hx, pol);
+  const float hz0 = ldm(m.hs + i - 1, pol), hzx0 = ldm(m.hs + i - ldz - 1, pol);
   pdl_wait();
   SWEEP_TMA(5, BOXZ)
   ldr<2>(f.szz + i, szz);
@@ -1348,8 +1386,9 @@ __device__ __forceinline__ void bwd_C_fast2(const SweepPack<K>& P, int shot, int
   const int rev = it >= 1;
   const float dt = g.dt;
   float sa[2], xa[2], za[2], bA[2], bB[2], vz[2], vx[2], gd[2], bBj[2];
-  ldr<2>(m.bycA + i, bA);
-  ldr<2>(m.bycB + i, bB);
+  const uint64_t pol = media_policy();
+  ldrm<2>(m.bycA + i, bA, pol);
+  ldrm<2>(m.bycB + i, bB, pol);
   pdl_wait();
   SWEEP_TMA(5, BOXZ)
   ldr<2>(f.szz_a + i, sa);
@@ -1361,8 +1400,8 @@ __device__ __forceinline__ void bwd_C_fast2(const SweepPack<K>& P, int shot, int
     ldr<2>(f.vz + i, vz);
     ldr<2>(f.vx + i, vx);
     ldr<2>(gr.den + i, gd);
-    ldr<2>(m.bycB + i - ldz, bBj);
-    bAj0 = m.bycA[i - 1];
+    ldrm<2>(m.bycB + i - ldz, bBj, pol);
+    bAj0 = ldm(m.bycA + i - 1, pol);
   }
   if (!stage_wait(&bar, err)) return;
   const float* s_vza = sm;
