@@ -1034,12 +1034,42 @@ __device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int 
   ldr<R>(gr.mu + i, gm);
   ldr<R>(f.vz_a + i, va_z);
   ldr<R>(f.vx_a + i, va_x);
-  if (!stage_wait(&bar, err)) return;
+  // Fast one-row tiles share the strain e = dvx_dz + dvz_dx of the mu
+  // gathers: each thread computes its own cell's, warp 0 the tile's x0 - 1
+  // column and z0 - 1 row, and the gathers read their neighbours' from
+  // shared memory (s_e: columns x0 - 1 .. x0 + TX - 1, depths z0 - 1 ..
+  // z0 + 31, stride 33) instead of recomputing them. Same operations per value.
+  constexpr bool kShare = !MID && R == 1;
+  const bool ok = stage_wait(&bar, err);
+  if constexpr (kShare) {
+    if (!__syncthreads_and(ok)) return;  // (a uniform exit: the block meets a barrier below)
+  } else {
+    if (!ok) return;
+  }
   const float* s_vz = sm;
   const float* s_vx = sm + N;
   const float* s_szz_a = sm + 2 * N;
   const float* s_sxx_a = sm + 3 * N;
   const float* s_sxz_a = sm + 4 * N;
+  float e_me = 0.0f, e_up = 0.0f, e_left = 0.0f, e_upleft = 0.0f;
+  if constexpr (kShare) {
+    float* s_e = sm + 5 * N;
+    const int ty = threadIdx.y, tx = threadIdx.x;
+    e_me = sdp(s_vx, b, 1, g.rdz) + sdp(s_vz, b, BOXZ, g.rdx);
+    s_e[(ty + 1) * 33 + tx + 1] = e_me;
+    if (ty == 0) {
+      const int bl = b - BOXZ;  // (z, x0 - 1)
+      s_e[tx + 1] = sdp(s_vx, bl, 1, g.rdz) + sdp(s_vz, bl, BOXZ, g.rdx);
+      if (tx <= TX) {
+        const int bu = (tx + 1) * BOXZ + 3;  // (z0 - 1, x0 - 1 + tx)
+        s_e[tx * 33] = sdp(s_vx, bu, 1, g.rdz) + sdp(s_vz, bu, BOXZ, g.rdx);
+      }
+    }
+    __syncthreads();
+    e_up = s_e[(ty + 1) * 33 + tx];
+    e_left = s_e[ty * 33 + tx + 1];
+    e_upleft = s_e[ty * 33 + tx];
+  }
   float o_gl[R], o_gm[R], o_szz[R], o_sxx[R], o_sxz[R], o_vza[R], o_vxa[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
@@ -1054,13 +1084,14 @@ __device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int 
     const bool inter = !MID || in_box(zr, x, g.zi0, g.zi1, g.xi0, g.xi1);
     const float dvz_dz = sdm(s_vz, bb, 1, g.rdz);
     const float dvx_dx = sdm(s_vx, bb, BOXZ, g.rdx);
-    const float dvx_dz = sdp(s_vx, bb, 1, g.rdz);
-    const float dvz_dx = sdp(s_vz, bb, BOXZ, g.rdx);
     float e_own = 0.0f, gmu_own = 0.0f;
     if (inter) {
       o_szz[r] = szz[r] - (l2m[r] * dvz_dz + lam[r] * dvx_dx) * dt;
       o_sxx[r] = sxx[r] - (lam[r] * dvz_dz + l2m[r] * dvx_dx) * dt;
-      e_own = dvx_dz + dvz_dx;
+      if constexpr (kShare)
+        e_own = e_me;
+      else
+        e_own = sdp(s_vx, bb, 1, g.rdz) + sdp(s_vz, bb, BOXZ, g.rdx);  // dvx_dz + dvz_dx
       o_sxz[r] = sxz[r] - amu[r] * e_own * dt;
       const float sa = s_szz_a[bb], xa = s_sxx_a[bb];
       o_gl[r] = gl[r] + -(sa + xa) * (dvz_dz + dvx_dx) * dt * kMega;
@@ -1091,17 +1122,20 @@ __device__ __forceinline__ void bwd_B_fast(const SweepPack<K>& P, int shot, int 
         if (h[r] != 0.0f) acc += w[r] * (-s_sxz_a[bb] * e_own * dt * h[r]);
         if (up && hz != 0.0f) {
           const int bj = bb - 1;
-          acc += w[r] * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, BOXZ, g.rdx)) * dt * hz);
+          const float e = kShare ? e_up : sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, BOXZ, g.rdx);
+          acc += w[r] * (-s_sxz_a[bj] * e * dt * hz);
         }
       }
       if (left) {
         if (hx[r] != 0.0f) {
           const int bj = bb - BOXZ;
-          acc += w[r] * (-s_sxz_a[bj] * (sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, BOXZ, g.rdx)) * dt * hx[r]);
+          const float e = kShare ? e_left : sdp(s_vx, bj, 1, g.rdz) + sdp(s_vz, bj, BOXZ, g.rdx);
+          acc += w[r] * (-s_sxz_a[bj] * e * dt * hx[r]);
         }
         if (up && own_col && hzx != 0.0f) {
           const int b2 = bb - BOXZ - 1;
-          acc += w[r] * (-s_sxz_a[b2] * (sdp(s_vx, b2, 1, g.rdz) + sdp(s_vz, b2, BOXZ, g.rdx)) * dt * hzx);
+          const float e = kShare ? e_upleft : sdp(s_vx, b2, 1, g.rdz) + sdp(s_vz, b2, BOXZ, g.rdx);
+          acc += w[r] * (-s_sxz_a[b2] * e * dt * hzx);
         }
       }
       o_gm[r] = acc;
@@ -1932,6 +1966,12 @@ template <int TX, int BOXZ>
 constexpr size_t smem_bytes(int na) {
   return static_cast<size_t>(na) * BOXZ * (TX + 4) * sizeof(float);
 }
+// Backward sweep B, one-row tiles: the five staged boxes, then the strains its
+// fast bodies' mu gathers share ((TX + 1) columns x 33 depths).
+template <int TX>
+constexpr size_t bwd_B_smem_one_row() {
+  return smem_bytes<TX, kBoxZ>(5) + static_cast<size_t>((TX + 1) * 33) * sizeof(float);
+}
 
 }  // namespace
 
@@ -2009,10 +2049,10 @@ int launch_bwd_B(cudaStream_t s, int tx, int rows, int regs, const SweepPack<K>&
                                      smem_bytes<TX, kBoxZFwd>(5), s, p, j, err))
   else if (regs > 32)
     FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K, 1, 1536>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
-                                     smem_bytes<TX, kBoxZ>(5), s, p, j, err))
+                                     bwd_B_smem_one_row<TX>(), s, p, j, err))
   else
     FWIGB_DISPATCH_TX(tx, launch_pdl(k_bwd_B<TX, K, 1, 2048>, sweep_grid(TX, kTileZ, gr, nshots), dim3(32, TX),
-                                     smem_bytes<TX, kBoxZ>(5), s, p, j, err))
+                                     bwd_B_smem_one_row<TX>(), s, p, j, err))
   return 1;
 }
 
