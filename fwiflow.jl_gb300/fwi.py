@@ -241,7 +241,8 @@ class FwiContext:
         _lib.check(self._lib.fwigb_set_tile_rows(self._h, _lib.iptr(t)), self._h)
 
     def set_graphs(self, enable: bool) -> None:
-        """Replay a lone shot's launch sequence from a CUDA graph (default on)."""
+        """Replay a single-group call's launch sequence (a lone shot or a
+        batched group) from a CUDA graph (default on)."""
         _lib.check(self._lib.fwigb_set_graphs(self._h, int(enable)), self._h)
 
     def sweep_time(self, kind: int, reps: int = 50) -> float:
