@@ -45,7 +45,7 @@ typedef enum fwigb_status {
   FWIGB_ERR_OOM = 5,        /* device allocation failed */
   FWIGB_ERR_IO = 6,         /* observed-data or output file I/O failed */
   FWIGB_ERR_TIMEOUT = 7,    /* a bounded device wait gave up: the call's outputs are undefined */
-  FWIGB_ERR_UNSUPPORTED = 8 /* option of the parameter file this build does not implement */
+  FWIGB_ERR_UNSUPPORTED = 8 /* option of the parameter file the library does not implement */
 } fwigb_status;
 
 typedef struct fwigb_ctx fwigb_ctx;
