@@ -67,6 +67,8 @@ SIGNATURES = {
     "fwigb_set_batching": ([_V, ctypes.c_int, ctypes.c_ulonglong], ctypes.c_int),
     "fwigb_last_group_count": ([_V], ctypes.c_int),
     "fwigb_set_illumination": ([_V, ctypes.c_int], ctypes.c_int),
+    "fwigb_misfit_gathers_noalloc": ([_V, _V, _V, ctypes.c_int, ctypes.c_int, ctypes.c_float, _D, _V], ctypes.c_int),
+    "fwigb_noalloc_last_error": ([], ctypes.c_char_p),
     "fwigb_test_inject_wait_timeout": ([_V, ctypes.c_int], ctypes.c_int),
     "fwigb_fetch_illumination": ([_V, _D], ctypes.c_int),
     "fwigb_cnn_conv3x3": ([_V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _V, _V, _V, _V,

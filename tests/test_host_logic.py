@@ -86,6 +86,15 @@ def test_library_exports_every_header_symbol(fw):
     assert not missing, missing
 
 
+def test_every_header_function_has_a_python_signature(fw):
+    """The ctypes table covers the whole C ABI (argument and result types of
+    every function in include/fwiflow_gb300.h)."""
+    from fwiflow_gb300 import _lib
+
+    missing = [n for n in _header_functions() if n not in _lib.SIGNATURES]
+    assert not missing, missing
+
+
 def test_create_reports_parameter_errors_without_gpu(fw, tmp_path):
     """Parameter problems are reported as FWIGB_ERR_PARAM before any CUDA call
     (the reference asserts or exits, Parameter.cpp:35-116)."""
